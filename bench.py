@@ -1,0 +1,291 @@
+"""EMST throughput benchmark (one JSON line on stdout).
+
+Default workload: gauss3d_1e7 -- 10,000,000 3D points, 90% from 256 anisotropic
+Gaussian clusters + 10% uniform background (seed 5), the plain Boruvka EMST.
+  value   Mpoints/s with the points already in HBM (emst_solve_device), device
+          time by CUDA events on the library's stream, L2 flushed between steps
+  e2e     Mpoints/s through emst_solve with pinned host points in and host
+          edges + length out (H2D and D2H inside the timed region)
+  roofline  the static-pruning region-table kernel (k_nns): algorithmic bytes
+          N*(4*D + 8*K) per launch / its CUDA-event time, against the measured
+          HBM copy bandwidth
+  cpu_baseline  the oracle (CPU restatement of the reference's algorithm)
+          on a bounded sample of the same workload, 1 thread
+
+--impl reference: the CPU restatement of the reference's path (oracle port,
+OpenMP over all host cores), each step a bounded sample of the same workload.
+Under torchrun (N > 1) every rank solves its own replica ("replicas only").
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "component-based-2d-3d-nns-to-gpu-parallel-2d-3d-emst_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "EMST Mpoints/s at 1e7 pts (plain Boruvka, exact edge set); % HBM roofline"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 8:
+                self.rows.append(f)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for f in self.rows:
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def nns_bytes(n, dim):
+    """Algorithmic bytes of one region-table launch: read the sorted points once
+    (4*D per point) and write K (id, d2) pairs (8*K per point)."""
+    K = 8 if dim == 2 else 24
+    return n * (4 * dim + 8 * K)
+
+
+def traffic_from_profile(name, n):
+    """dram bytes per point of k_nns from the committed ncu summary, scaled to n."""
+    path = os.path.join(ROOT, "profiles", "k_nns_%s.md" % name)
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_point:"):
+                return float(line.split(":")[1]) * n
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(pts, threads, sample_n, seed=0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(pts), min(sample_n, len(pts)), replace=False)
+    sub = np.ascontiguousarray(pts[np.sort(idx)])
+    O.set_threads(threads)
+    sp, _, _, _ = O.rescale(sub)
+    t0 = time.perf_counter()
+    r = O.emst(sp, "faithful")
+    dt = time.perf_counter() - t0
+    assert len(r.edges) == len(sub) - 1
+    return len(sub) / dt / 1e6, dt, len(sub)
+
+
+def run_reference(args, pts, dim):
+    """The CPU restatement of the reference's path, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    threads = os.cpu_count() or 1
+    sample_n = args.ref_sample
+    for _ in range(args.warmup):
+        cpu_baseline(pts, threads, min(sample_n, 20000), seed=1)
+    times, npts = [], 0
+    for s in range(args.steps):
+        v, dt, m = cpu_baseline(pts, threads, sample_n, seed=100 + s)
+        times.append(dt)
+        npts += m
+    total = sum(times)
+    value = npts / total / 1e6
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": args.workload, "n": len(pts), "dim": dim},
+            "cpu_baseline": {"value": value, "unit": "Mpoints/s", "cores": threads, "kind": "port",
+                             "sample": "%d random points of %s per step (CPU restatement of the reference's "
+                                       "ring-search static pruning + Boruvka, OpenMP)" % (sample_n, args.workload)},
+            "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="gauss3d_1e7")
+    ap.add_argument("--n", type=int, default=None, help="override the workload size")
+    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--ref-sample", type=int, default=400_000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import emst_workloads as W
+    pts = W.make(args.workload, args.n)
+    n, dim = pts.shape
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, pts, dim)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    import emst_gb300 as E
+
+    dev_pts = torch.from_numpy(pts).cuda()
+    d_uv = torch.empty((max(n - 1, 1), 2), dtype=torch.int32, device="cuda")
+    d_len = torch.empty(1, dtype=torch.float64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    ctx = E.Emst(device=local, profile=True)
+    ctx.set_stream(stream.cuda_stream)
+
+    def step():
+        return ctx.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    dev_ms, nns_ms, launches, nns_launches, rounds = [], 0.0, 0, 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        ne = step()
+        ev1.record(stream)
+        ev1.synchronize()
+        dev_ms.append(ev0.elapsed_time(ev1))
+        prof = ctx.profile()
+        nns_ms += prof["ms_octants"]
+        launches += prof["launches"]
+        nns_launches += prof["octant_launches"]
+        rounds = prof["rounds"]
+        assert ne == n - 1
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    total_ms = sum(dev_ms)
+    if dist is not None:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms / 1e3) / 1e6
+
+    # e2e through the public host API: pinned points in, host edges + length out
+    host_pts = torch.from_numpy(pts).pin_memory().numpy()
+    host_uv = torch.empty((max(n - 1, 1), 2), dtype=torch.int32).pin_memory().numpy()
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.solve_into(host_pts, host_uv)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ne, length = ctx.solve_into(host_pts, host_uv)
+        e2e_s += time.perf_counter() - t0
+    e2e = world * n * args.steps / e2e_s / 1e6
+
+    peak, peak_kind = peaks()
+    per_launch_ms = nns_ms / max(nns_launches, 1)
+    alg = nns_bytes(n, dim)
+    achieved = alg / (per_launch_ms / 1e3) / 1e9
+    traffic = traffic_from_profile(args.workload, n)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, m = cpu_baseline(pts, 1, args.cpu_sample)
+        cpu = {"value": v, "unit": "Mpoints/s", "cores": 1, "kind": "port",
+               "sample": "%d random points of %s (%.1f s), CPU restatement of the reference's ring-search static "
+                         "pruning + Boruvka, single thread" % (m, args.workload, dt)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": args.workload, "n": n, "dim": dim, "rounds": rounds,
+                           "l2": "512 MB buffer written between timed steps; working set > 129 MB L2",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "kernel": "k_nns",
+                             "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
+                             "peak_kind": peak_kind},
+                "cpu_baseline": cpu,
+                "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
+                        "d2h_bytes_per_step": int(8 * (n - 1) + 8)},
+                "gpu_launches": launches, "clocks": clocks,
+                "phase_ms_per_step": {k: v / args.steps for k, v in []}}
+        line.pop("phase_ms_per_step")
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

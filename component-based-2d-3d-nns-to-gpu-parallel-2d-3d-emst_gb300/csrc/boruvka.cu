@@ -1,0 +1,405 @@
+// boruvka.cu -- the per-round Boruvka operators.
+//
+//   select   (K_findNextClosestPoint, NodeEMST.h:1303-1384): each active point
+//            advances a cursor over its sorted region list past entries that
+//            are already in its component (they stay inside for good), takes
+//            the first outside entry -- the minimum by (d2, input id) -- and
+//            folds the edge key (d2 bits << 32 | min input id) into its root's
+//            slot with one 64-bit atomicMin.  Points whose whole list is inside
+//            leave the active list.
+//   resolve  (K_createComponentList + K_findMinPair, NodeEMST.h:817-955):
+//            the third key of the order (max input id) and the winner point
+//            are settled by a second 64-bit atomicMin, only over points whose
+//            atomicMin saw a value >= their own key (the final minimum is
+//            always among them).
+//   hook     (K_EMST_connectComponentAndUnion_2, EMSTOperators.h:1267-1303):
+//            a root hooks onto the root across its edge; for a mutual pair
+//            the root holding the lower input id stays root and that side
+//            emits the edge once.
+//   flatten  (K_EMST_flatten_DST_1, EMSTOperators.h:412-433): path-halving
+//            walk of the hooked roots, then every point's label is replaced
+//            by its root's root; surviving roots are compacted.
+#include "emst_ctx.h"
+#include "emst_device.cuh"
+
+namespace emst {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// Warp-aggregated append of `val` to list[] through counter *cnt.
+__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* list, uint32_t* cnt)
+{
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (uint32_t)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+__global__ void k_init(uint32_t n, uint32_t* __restrict__ lab, uint32_t* __restrict__ par,
+                       uint32_t* __restrict__ roots, uint32_t* __restrict__ act, uint64_t* __restrict__ ckey,
+                       uint64_t* __restrict__ cmax)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    lab[i] = i;
+    par[i] = i;
+    roots[i] = i;
+    act[i] = i;
+    ckey[i] = kNoKey;
+    cmax[i] = kNoKey;
+}
+
+template <int K>
+__global__ void k_select(const uint32_t* __restrict__ act, const uint32_t* __restrict__ n_act,
+                         const uint64_t* __restrict__ cand, const unsigned char* __restrict__ cnt,
+                         unsigned char* __restrict__ cur, const unsigned char* __restrict__ zflag,
+                         const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
+                         uint64_t* __restrict__ ckey, uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey,
+                         uint32_t* __restrict__ act_next, uint32_t* __restrict__ n_act_next,
+                         uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov)
+{
+    const uint32_t total = *n_act;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool keep = false, record = false;
+        uint32_t p = 0;
+        if (i < total) {
+            p = act[i];
+            const uint32_t lp = lab[p];
+            unsigned c = cur[p];
+            const unsigned m = cnt[p];
+            const uint64_t* L = cand + (uint64_t)p * K;
+            uint64_t e = 0;
+            uint32_t q = 0;
+            while (c < m) {
+                e = L[c];
+                q = (uint32_t)e;
+                if (lab[q] != lp) break;
+                ++c;
+            }
+            if (c != cur[p]) cur[p] = (unsigned char)c;
+            const bool found = c < m;
+            keep = found || zflag[p];
+            if (found) {
+                const uint32_t op = perm[p], oq = perm[q];
+                const uint64_t key = (e & 0xFFFFFFFF00000000ull) | (uint64_t)min(op, oq);
+                selq[p] = q;
+                selkey[p] = key;
+                if (key <= __ldcg(&ckey[lp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[lp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            }
+        }
+        warp_append(keep, p, act_next, n_act_next);
+        warp_append(record, p, prov, n_prov);
+    }
+}
+
+__global__ void k_resolve(const uint32_t* __restrict__ prov, const uint32_t* __restrict__ n_prov,
+                          const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
+                          const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ selq,
+                          const uint64_t* __restrict__ selkey, uint64_t* __restrict__ cmax)
+{
+    const uint32_t total = *n_prov;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t p = prov[i];
+        const uint32_t lp = lab[p];
+        if (selkey[p] != ckey[lp]) continue;
+        const uint32_t mx = max(perm[p], perm[selq[p]]);
+        atomicMin((unsigned long long*)&cmax[lp], (unsigned long long)(((uint64_t)mx << 32) | p));
+    }
+}
+
+__global__ void k_hook(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+                       const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
+                       const uint64_t* __restrict__ ckey, const uint64_t* __restrict__ cmax,
+                       const uint32_t* __restrict__ selq, uint32_t* __restrict__ par, int32_t* __restrict__ edges,
+                       int32_t* __restrict__ eround, uint32_t* __restrict__ n_edges, int round, uint32_t n,
+                       uint32_t* __restrict__ err)
+{
+    const uint32_t total = *n_roots;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool emit = false;
+        uint32_t u = 0, v = 0;
+        if (i < total) {
+            const uint32_t c = roots[i];
+            const uint64_t ck = ckey[c];
+            const uint64_t cm = cmax[c];
+            if (ck != kNoKey && (cm == kNoKey || (uint32_t)cm >= n)) {
+                atomicOr(err, 2u);  // a root with an edge key but no winner: internal error
+            } else if (ck != kNoKey) {
+                const uint32_t w = (uint32_t)cm;
+                const uint32_t q = selq[w];
+                const uint32_t cq = lab[q];
+                const bool mutual = ckey[cq] == ck && (cmax[cq] >> 32) == (cm >> 32);
+                const uint32_t ow = perm[w], oq = perm[q];
+                if (!mutual || ow > oq) par[c] = cq;
+                emit = !mutual || ow < oq;
+                u = min(ow, oq);
+                v = max(ow, oq);
+            }
+        }
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, emit);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            uint32_t b = 0;
+            if (lane == leader) b = atomicAdd(n_edges, (uint32_t)__popc(m));
+            b = __shfl_sync(act, b, leader);
+            const uint32_t k = b + __popc(m & ((1u << lane) - 1u));
+            if (emit && k + 1 >= n) atomicOr(err, 4u);  // more than n - 1 edges: internal error
+            if (emit && k + 1 < n) {
+                edges[2 * (uint64_t)k] = (int32_t)u;
+                edges[2 * (uint64_t)k + 1] = (int32_t)v;
+                eround[k] = round;
+            }
+        }
+    }
+}
+
+// Path-halving walk from every previous root to its new root.  The hook
+// graph is acyclic, so a walk ends within n_roots steps; the step cap only
+// turns an internal error into an error flag instead of an endless loop.
+__global__ void k_jump(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+                       uint32_t* __restrict__ par, uint32_t* __restrict__ err)
+{
+    const uint32_t total = *n_roots;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t c = roots[i];
+        uint32_t x = c;
+        for (uint32_t step = 0;; ++step) {
+            if (step > total) {
+                atomicOr(err, 8u);
+                break;
+            }
+            const uint32_t y = __ldcg(&par[x]);
+            if (y == x) break;
+            const uint32_t z = __ldcg(&par[y]);
+            if (z == y) {
+                x = y;
+                break;
+            }
+            // Halve only if x still points at y: a plain store could overwrite
+            // another thread's final par[x] = root with the stale ancestor z.
+            atomicCAS(&par[x], y, z);
+            x = z;
+        }
+        if (x != c) par[c] = x;
+    }
+}
+
+__global__ void k_relabel(uint32_t n, uint32_t* __restrict__ lab, const uint32_t* __restrict__ par)
+{
+    uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i + 3 < n) {
+        uint4 l = *reinterpret_cast<uint4*>(lab + i);
+        l.x = __ldcg(&par[l.x]);
+        l.y = __ldcg(&par[l.y]);
+        l.z = __ldcg(&par[l.z]);
+        l.w = __ldcg(&par[l.w]);
+        *reinterpret_cast<uint4*>(lab + i) = l;
+    } else {
+        for (; i < n; ++i) lab[i] = __ldcg(&par[lab[i]]);
+    }
+}
+
+__global__ void k_compact_roots(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+                                const uint32_t* __restrict__ par, uint64_t* __restrict__ ckey,
+                                uint64_t* __restrict__ cmax, uint32_t* __restrict__ roots_next,
+                                uint32_t* __restrict__ n_roots_next)
+{
+    const uint32_t total = *n_roots;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool keep = false;
+        uint32_t c = 0;
+        if (i < total) {
+            c = roots[i];
+            keep = par[c] == c;
+            if (keep) {
+                ckey[c] = kNoKey;
+                cmax[c] = kNoKey;
+            }
+        }
+        warp_append(keep, c, roots_next, n_roots_next);
+    }
+}
+
+__global__ void k_count_other(uint32_t n, const uint32_t* __restrict__ lab, const uint32_t* __restrict__ pos0,
+                              uint32_t* __restrict__ out)
+{
+    const uint32_t r0 = lab[*pos0];
+    uint32_t cnt = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) cnt += lab[i] != r0;
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(out, cnt);
+}
+
+template <int D>
+__global__ void k_edge_len(const int32_t* __restrict__ edges, uint32_t ne, const float* __restrict__ in,
+                           double* __restrict__ part)
+{
+    __shared__ double s[256 / 32];
+    double acc = 0.0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+        const int64_t u = edges[2 * (uint64_t)e], v = edges[2 * (uint64_t)e + 1];
+        const float dx = __fsub_rn(in[u * D], in[v * D]);
+        const float dy = __fsub_rn(in[u * D + 1], in[v * D + 1]);
+        const float dz = D == 3 ? __fsub_rn(in[u * D + 2], in[v * D + 2]) : 0.f;
+        acc += sqrt((double)d2_of<D>(dx, dy, dz));
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int j = 0; j < (int)(blockDim.x / 32); ++j) t += s[j];
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_sum_parts(const double* __restrict__ part, int nb, double* __restrict__ out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (int j = 0; j < nb; ++j) t += part[j];
+        *out = t;
+    }
+}
+
+__global__ void k_labels_out(uint32_t n, const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
+                             int32_t* __restrict__ out)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    out[perm[p]] = (int32_t)perm[lab[p]];
+}
+
+unsigned list_grid(uint64_t upper)
+{
+    uint64_t b = (upper + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 152ull * 16) b = 152ull * 16;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+cudaError_t boruvka_init(Ctx& c)
+{
+    cudaError_t e;
+    const size_t n = (size_t)c.n;
+    if ((e = ensure(c.lab, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.par, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.selq, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.selkey, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.ckey, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.cmax, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.act, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.act2, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.roots, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.roots2, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.prov, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.edges, 2 * (n > 1 ? n - 1 : 1))) != cudaSuccess) return e;
+    if ((e = ensure(c.eround, n > 1 ? n - 1 : 1)) != cudaSuccess) return e;
+    k_init<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.par.p, c.roots.p, c.act.p,
+                                                        c.ckey.p, c.cmax.p);
+    c.n_act = (uint32_t)c.n;
+    c.n_roots = (uint32_t)c.n;
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t boruvka_flatten(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    k_jump<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->n_roots, c.par.p, &d->err);
+    k_relabel<<<blocks_for((c.n + 3) / 4, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.par.p);
+    cudaMemcpyAsync(&d->s_roots, &d->n_roots, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemsetAsync(&d->n_roots, 0, sizeof(uint32_t), c.stream);
+    k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->s_roots, c.par.p, c.ckey.p, c.cmax.p,
+                                                                c.roots2.p, &d->n_roots);
+    std::swap(c.roots.p, c.roots2.p);
+    c.launches += 3;
+    return cudaGetLastError();
+}
+
+cudaError_t boruvka_select(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    cudaMemcpyAsync(&d->s_act, &d->n_act, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemsetAsync(&d->n_act, 0, sizeof(uint32_t), c.stream);
+    cudaMemsetAsync(&d->n_prov, 0, sizeof(uint32_t), c.stream);
+    const unsigned g = list_grid(c.n_act);
+    if (c.dim == 2)
+        k_select<8><<<g, 256, 0, c.stream>>>(c.act.p, &d->s_act, c.cand.p, c.cnt.p, c.cur.p, c.zflag.p, c.lab.p,
+                                             c.perm.p, c.ckey.p, c.selq.p, c.selkey.p, c.act2.p, &d->n_act,
+                                             c.prov.p, &d->n_prov);
+    else
+        k_select<24><<<g, 256, 0, c.stream>>>(c.act.p, &d->s_act, c.cand.p, c.cnt.p, c.cur.p, c.zflag.p, c.lab.p,
+                                              c.perm.p, c.ckey.p, c.selq.p, c.selkey.p, c.act2.p, &d->n_act,
+                                              c.prov.p, &d->n_prov);
+    std::swap(c.act.p, c.act2.p);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t boruvka_resolve(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    k_resolve<<<list_grid(c.n_act), 256, 0, c.stream>>>(c.prov.p, &d->n_prov, c.lab.p, c.perm.p, c.ckey.p, c.selq.p,
+                                                         c.selkey.p, c.cmax.p);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t boruvka_hook(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    k_hook<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->n_roots, c.lab.p, c.perm.p, c.ckey.p, c.cmax.p,
+                                                       c.selq.p, c.par.p, c.edges.p, c.eround.p, &d->n_edges,
+                                                       c.round, (uint32_t)c.n, &d->err);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t boruvka_count_other(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    cudaMemsetAsync(&d->n_other, 0, sizeof(uint32_t), c.stream);
+    k_count_other<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, &d->pos0, &d->n_other);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t evaluate_length(Ctx& c, double* d_out)
+{
+    cudaError_t e;
+    const unsigned nb = list_grid(c.n_edges ? c.n_edges : 1);
+    if ((e = ensure(c.lpart, nb)) != cudaSuccess) return e;
+    if (c.dim == 2)
+        k_edge_len<2><<<nb, 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.in, c.lpart.p);
+    else
+        k_edge_len<3><<<nb, 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.in, c.lpart.p);
+    k_sum_parts<<<1, 32, 0, c.stream>>>(c.lpart.p, (int)nb, d_out);
+    c.launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out)
+{
+    k_labels_out<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.perm.p, d_out);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace emst

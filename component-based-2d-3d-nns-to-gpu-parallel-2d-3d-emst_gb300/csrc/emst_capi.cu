@@ -1,0 +1,572 @@
+// emst_capi.cu -- the C ABI (include/emst.h) and the host-side round driver.
+//
+// The operator sequence and its stage checks follow SolutionEMST::activate
+// (emst_coalition/src/SolutionEMSTOperators.cu:156-422): flatten, termination
+// test, iteration++, find-min-1 (computeOctants + findNextClosestPoint),
+// find-min-2 (component min pair), connect-and-union; the loop stops when one
+// component remains or at the 100-round cap (:210).
+#include <cstring>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/emst.h"
+#include "emst_ctx.h"
+
+struct emst_ctx {
+    emst::Ctx c;
+    int stage = 0;  // 0: needs flatten, 1: flattened, 2: octants, 3: next-closest, 4: min-pair
+    int64_t last_edges = 0;
+    emst::DevBuf<int32_t> tmp_i32;
+    // phase timing: (phase, start, end) event pairs recorded since the last sync
+    struct Pending {
+        int phase;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
+    double ms[6] = {0, 0, 0, 0, 0, 0};
+};
+
+namespace {
+
+using emst::Ctx;
+
+enum { PH_GRID = 0, PH_OCTANTS, PH_SELECT, PH_RESOLVE, PH_HOOK, PH_FLATTEN };
+
+// Records CUDA events around one operator on the context's stream.
+struct Timed {
+    emst_ctx* x;
+    int ph;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Timed(emst_ctx* x_, int ph_) : x(x_), ph(ph_)
+    {
+        if (!x->c.profile) return;
+        if (x->pool.empty()) {
+            cudaEvent_t e0, e1;
+            if (cudaEventCreate(&e0) != cudaSuccess) return;
+            if (cudaEventCreate(&e1) != cudaSuccess) {
+                cudaEventDestroy(e0);
+                return;
+            }
+            x->pool.push_back({e0, e1});
+        }
+        a = x->pool.back().first;
+        b = x->pool.back().second;
+        x->pool.pop_back();
+        cudaEventRecord(a, x->c.stream);
+    }
+    ~Timed()
+    {
+        if (!a) return;
+        cudaEventRecord(b, x->c.stream);
+        x->pending.push_back({ph, a, b});
+    }
+};
+
+// After a stream synchronisation: fold the recorded phase times in.
+void harvest(emst_ctx* x)
+{
+    for (auto& p : x->pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) x->ms[p.phase] += ms;
+        x->pool.push_back({p.a, p.b});
+    }
+    x->pending.clear();
+    cudaGetLastError();
+}
+
+emst_status set_err(emst_ctx* x, emst_status st, const std::string& msg)
+{
+    if (x) x->c.err = msg;
+    return st;
+}
+
+emst_status cuda_err(emst_ctx* x, cudaError_t e, const char* where)
+{
+    if (e == cudaSuccess) return EMST_OK;
+    cudaGetLastError();  // clear a sticky launch error where possible
+    return set_err(x, e == cudaErrorMemoryAllocation ? EMST_ENOMEM : EMST_ECUDA,
+                   std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define EMST_CUDA(x, call, where)                                  \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return cuda_err((x), _e, (where));  \
+    } while (0)
+
+emst_status read_counters(emst_ctx* x)
+{
+    Ctx& c = x->c;
+    EMST_CUDA(x, cudaMemcpyAsync(c.hctr, c.ctr.p, sizeof(emst::DevCounters), cudaMemcpyDeviceToHost, c.stream),
+              "counters");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+    harvest(x);
+    c.n_act = c.hctr->n_act;
+    c.n_roots = c.hctr->n_roots;
+    c.n_zero = c.hctr->n_zero_next;
+    c.n_edges = c.hctr->n_edges;
+    if (c.hctr->err & 1u) return set_err(x, EMST_EINVAL, "non-finite input coordinate");
+    if (c.hctr->err) return set_err(x, EMST_ECUDA, "internal consistency check failed (flags " +
+                                               std::to_string(c.hctr->err) + ")");
+    return EMST_OK;
+}
+
+emst_status check_ready(emst_ctx* x)
+{
+    if (!x) return EMST_EINVAL;
+    if (x->c.phase == 0) return set_err(x, EMST_ESTATE, "emst_initialize has not been called");
+    EMST_CUDA(x, cudaSetDevice(x->c.device), "cudaSetDevice");
+    return EMST_OK;
+}
+
+emst_status do_flatten(emst_ctx* x)
+{
+    Ctx& c = x->c;
+    if (x->stage != 0) return set_err(x, EMST_ESTATE, "flatten: previous round not finished");
+    if (c.round > 0) {
+        Timed t(x, PH_FLATTEN);
+        EMST_CUDA(x, emst::boruvka_flatten(c), "flatten");
+    }
+    emst_status st = read_counters(x);
+    if (st != EMST_OK) return st;
+    if (c.round > (int)c.cum_edges.size()) c.cum_edges.push_back(c.n_edges);
+    x->stage = 1;
+    return EMST_OK;
+}
+
+emst_status do_octants(emst_ctx* x)
+{
+    Ctx& c = x->c;
+    if (x->stage != 1) return set_err(x, EMST_ESTATE, "compute_octants: call flatten first");
+    c.round++;
+    Timed t(x, PH_OCTANTS);
+    if (c.round == 1)
+        EMST_CUDA(x, emst::nns_full(c), "compute_octants");
+    else
+        EMST_CUDA(x, emst::nns_recompute_zero(c), "compute_octants (zero recompute)");
+    x->stage = 2;
+    return EMST_OK;
+}
+
+emst_status do_select(emst_ctx* x)
+{
+    if (x->stage != 2) return set_err(x, EMST_ESTATE, "find_next_closest: call compute_octants first");
+    Timed t(x, PH_SELECT);
+    EMST_CUDA(x, emst::boruvka_select(x->c), "find_next_closest");
+    x->stage = 3;
+    return EMST_OK;
+}
+
+emst_status do_resolve(emst_ctx* x)
+{
+    if (x->stage != 3) return set_err(x, EMST_ESTATE, "find_min_pair: call find_next_closest first");
+    Timed t(x, PH_RESOLVE);
+    EMST_CUDA(x, emst::boruvka_resolve(x->c), "find_min_pair");
+    x->stage = 4;
+    return EMST_OK;
+}
+
+emst_status do_hook(emst_ctx* x)
+{
+    if (x->stage != 4) return set_err(x, EMST_ESTATE, "connect_union: call find_min_pair first");
+    Timed t(x, PH_HOOK);
+    EMST_CUDA(x, emst::boruvka_hook(x->c), "connect_union");
+    x->stage = 0;
+    return EMST_OK;
+}
+
+emst_status do_activate(emst_ctx* x, int* more)
+{
+    Ctx& c = x->c;
+    *more = 0;
+    if (c.finished) return EMST_OK;
+    emst_status st = do_flatten(x);
+    if (st != EMST_OK) return st;
+    if (c.n_roots <= 1) {
+        c.finished = true;
+        x->stage = 0;
+        return EMST_OK;
+    }
+    if (c.round > 0 && (int64_t)c.n_edges == x->last_edges) {
+        c.finished = true;
+        x->stage = 0;
+        return set_err(x, EMST_ENOCONVERGE, "a round added no edge while several components remain");
+    }
+    if (c.round == c.max_rounds) {
+        c.finished = true;
+        x->stage = 0;
+        return set_err(x, EMST_ENOCONVERGE, "round cap reached");
+    }
+    x->last_edges = c.n_edges;
+    if ((st = do_octants(x)) != EMST_OK) return st;
+    if ((st = do_select(x)) != EMST_OK) return st;
+    if ((st = do_resolve(x)) != EMST_OK) return st;
+    if ((st = do_hook(x)) != EMST_OK) return st;
+    *more = 1;
+    return EMST_OK;
+}
+
+emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, int is_device)
+{
+    Ctx& c = x->c;
+    if (!points) return set_err(x, EMST_EINVAL, "points is NULL");
+    if (dim != 2 && dim != 3) return set_err(x, EMST_EINVAL, "dim must be 2 or 3");
+    if (n < 1) return set_err(x, EMST_EINVAL, "n must be >= 1");
+    if (n >= (int64_t)0x7fffffff) return set_err(x, EMST_EOVERFLOW, "n must be < 2^31 - 1");
+    EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
+    if (!is_device) {
+        EMST_CUDA(x, emst::ensure(c.in_own, (size_t)n * dim), "alloc points");
+        EMST_CUDA(x, cudaMemcpyAsync(c.in_own.p, points, sizeof(float) * n * dim, cudaMemcpyHostToDevice, c.stream),
+                  "upload points");
+        c.in = c.in_own.p;
+    } else {
+        c.in = points;
+    }
+    c.n = n;
+    c.dim = dim;
+    c.K = dim == 2 ? 8 : 24;
+    std::memset(c.hctr, 0, sizeof(emst::DevCounters));
+    c.hctr->n_act = (uint32_t)n;
+    c.hctr->n_roots = (uint32_t)n;
+    EMST_CUDA(x, cudaMemcpyAsync(c.ctr.p, c.hctr, sizeof(emst::DevCounters), cudaMemcpyHostToDevice, c.stream),
+              "counters");
+    c.launches = 0;
+    c.nns_launches = 0;
+    for (double& v : x->ms) v = 0.0;
+    {
+        Timed t(x, PH_GRID);
+        EMST_CUDA(x, emst::grid_build(c), "grid build");
+        EMST_CUDA(x, emst::boruvka_init(c), "init");
+    }
+    c.round = 0;
+    c.finished = false;
+    c.n_edges = 0;
+    c.n_zero = 0;
+    c.cum_edges.clear();
+    c.phase = 1;
+    x->stage = 0;
+    x->last_edges = 0;
+    return EMST_OK;
+}
+
+emst_status do_run(emst_ctx* x)
+{
+    int more = 1;
+    while (more) {
+        emst_status st = do_activate(x, &more);
+        if (st != EMST_OK) return st;
+    }
+    return EMST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+emst_status emst_create(const emst_config* cfg, emst_ctx** out)
+{
+    if (!out) return EMST_EINVAL;
+    *out = nullptr;
+    emst_ctx* x = new (std::nothrow) emst_ctx();
+    if (!x) return EMST_ENOMEM;
+    Ctx& c = x->c;
+    if (cfg) {
+        c.device = cfg->device;
+        if (cfg->max_rounds > 0) c.max_rounds = cfg->max_rounds;
+        if (cfg->warps_per_block > 0) c.warps_per_block = cfg->warps_per_block;
+        c.keep_table = cfg->keep_region_table != 0;
+        c.profile = cfg->profile != 0;
+    }
+    cudaError_t e = cudaSetDevice(c.device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = emst::ensure(c.ctr, 1);
+    if (e == cudaSuccess) e = emst::ensure(c.dlen, 1);
+    if (e == cudaSuccess) e = cudaMallocHost(&c.hctr, sizeof(emst::DevCounters));
+    if (e == cudaSuccess) e = cudaMallocHost(&c.hlen, sizeof(double));
+    if (e != cudaSuccess) {
+        emst_destroy(x);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? EMST_ENOMEM : EMST_ECUDA;
+    }
+    c.stream = c.own_stream;
+    *out = x;
+    return EMST_OK;
+}
+
+emst_status emst_destroy(emst_ctx* x)
+{
+    if (!x) return EMST_OK;
+    Ctx& c = x->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    emst::release(c.in_own);
+    emst::release(c.scaled);
+    emst::release(c.sp);
+    emst::release(c.perm);
+    emst::release(c.perm_alt);
+    emst::release(c.mkey);
+    emst::release(c.mkey_alt);
+    emst::release(c.sort_tmp);
+    emst::release(c.part);
+    emst::release(c.norm);
+    emst::release(c.nlo);
+    emst::release(c.nhi);
+    emst::release(c.nid);
+    emst::release(c.cand);
+    emst::release(c.cnt);
+    emst::release(c.cur);
+    emst::release(c.zflag);
+    emst::release(c.tab_id);
+    emst::release(c.tab_d2);
+    emst::release(c.lab);
+    emst::release(c.par);
+    emst::release(c.selq);
+    emst::release(c.ckey);
+    emst::release(c.cmax);
+    emst::release(c.selkey);
+    emst::release(c.act);
+    emst::release(c.act2);
+    emst::release(c.roots);
+    emst::release(c.roots2);
+    emst::release(c.prov);
+    emst::release(c.zero);
+    emst::release(c.zero2);
+    emst::release(c.edges);
+    emst::release(c.eround);
+    emst::release(c.ctr);
+    emst::release(c.lpart);
+    emst::release(c.dlen);
+    emst::release(x->tmp_i32);
+    for (auto& p : x->pending) x->pool.push_back({p.a, p.b});
+    for (auto& p : x->pool) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    if (c.hctr) cudaFreeHost(c.hctr);
+    if (c.hlen) cudaFreeHost(c.hlen);
+    if (c.own_stream) cudaStreamDestroy(c.own_stream);
+    delete x;
+    return EMST_OK;
+}
+
+const char* emst_last_error(const emst_ctx* x) { return x ? x->c.err.c_str() : "null context"; }
+
+emst_status emst_set_stream(emst_ctx* x, void* stream)
+{
+    if (!x) return EMST_EINVAL;
+    x->c.stream = stream ? (cudaStream_t)stream : x->c.own_stream;
+    return EMST_OK;
+}
+
+emst_status emst_initialize(emst_ctx* x, const float* points, int64_t n, int dim, int points_are_device)
+{
+    if (!x) return EMST_EINVAL;
+    return do_initialize(x, points, n, dim, points_are_device);
+}
+
+emst_status emst_compute_octants(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_octants(x);
+}
+
+emst_status emst_find_next_closest(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_select(x);
+}
+
+emst_status emst_find_min_pair(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_resolve(x);
+}
+
+emst_status emst_connect_union(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_hook(x);
+}
+
+emst_status emst_flatten(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_flatten(x);
+}
+
+emst_status emst_test_termination(emst_ctx* x, int64_t* n_other)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    if (!n_other) return set_err(x, EMST_EINVAL, "n_other is NULL");
+    if (x->stage != 1) return set_err(x, EMST_ESTATE, "test_termination: call flatten first");
+    EMST_CUDA(x, emst::boruvka_count_other(x->c), "test_termination");
+    if ((st = read_counters(x)) != EMST_OK) return st;
+    *n_other = x->c.hctr->n_other;
+    return EMST_OK;
+}
+
+emst_status emst_activate(emst_ctx* x, int* more)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    int m = 0;
+    st = do_activate(x, &m);
+    if (more) *more = m;
+    return st;
+}
+
+emst_status emst_run(emst_ctx* x)
+{
+    emst_status st = check_ready(x);
+    return st != EMST_OK ? st : do_run(x);
+}
+
+emst_status emst_evaluate(emst_ctx* x, int64_t* n_edges, double* length)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if ((st = read_counters(x)) != EMST_OK) return st;
+    EMST_CUDA(x, emst::evaluate_length(c, c.dlen.p), "evaluate");
+    EMST_CUDA(x, cudaMemcpyAsync(c.hlen, c.dlen.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream), "evaluate");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "evaluate");
+    if (n_edges) *n_edges = c.n_edges;
+    if (length) *length = *c.hlen;
+    return EMST_OK;
+}
+
+emst_status emst_get_edges(emst_ctx* x, int32_t* uv, int32_t* round_of_edge, int64_t cap, int64_t* n_edges)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if ((st = read_counters(x)) != EMST_OK) return st;
+    if (n_edges) *n_edges = c.n_edges;
+    int64_t m = c.n_edges < (uint64_t)cap ? (int64_t)c.n_edges : cap;
+    if (m > 0 && uv)
+        EMST_CUDA(x, cudaMemcpyAsync(uv, c.edges.p, sizeof(int32_t) * 2 * m, cudaMemcpyDeviceToHost, c.stream),
+                  "get_edges");
+    if (m > 0 && round_of_edge)
+        EMST_CUDA(x, cudaMemcpyAsync(round_of_edge, c.eround.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, c.stream),
+                  "get_edges");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "get_edges");
+    if (cap < (int64_t)c.n_edges) return set_err(x, EMST_EOVERFLOW, "edge buffer too small");
+    return EMST_OK;
+}
+
+emst_status emst_get_labels(emst_ctx* x, int32_t* labels, int64_t cap)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (!labels || cap < c.n) return set_err(x, EMST_EOVERFLOW, "labels buffer too small");
+    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)c.n), "alloc");
+    EMST_CUDA(x, emst::labels_to_input_order(c, x->tmp_i32.p), "labels");
+    EMST_CUDA(x, cudaMemcpyAsync(labels, x->tmp_i32.p, sizeof(int32_t) * c.n, cudaMemcpyDeviceToHost, c.stream),
+              "labels");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "labels");
+    return EMST_OK;
+}
+
+emst_status emst_get_round_stats(emst_ctx* x, int64_t* rounds, int64_t* cum_edges, int64_t cap)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    const auto& v = x->c.cum_edges;
+    if (rounds) *rounds = (int64_t)v.size();
+    for (int64_t i = 0; cum_edges && i < cap && i < (int64_t)v.size(); ++i) cum_edges[i] = v[i];
+    return EMST_OK;
+}
+
+emst_status emst_get_region_table(emst_ctx* x, int32_t* ids, float* d2, int64_t cap)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (!c.keep_table) return set_err(x, EMST_ESTATE, "context created without keep_region_table");
+    if (c.round < 1) return set_err(x, EMST_ESTATE, "compute_octants has not run");
+    const int64_t m = c.n * c.K;
+    if (cap < m) return set_err(x, EMST_EOVERFLOW, "table buffer too small");
+    if (ids) EMST_CUDA(x, cudaMemcpyAsync(ids, c.tab_id.p, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, c.stream), "table");
+    if (d2) EMST_CUDA(x, cudaMemcpyAsync(d2, c.tab_d2.p, sizeof(float) * m, cudaMemcpyDeviceToHost, c.stream), "table");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "table");
+    return EMST_OK;
+}
+
+emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    if (!out) return set_err(x, EMST_EINVAL, "out is NULL");
+    EMST_CUDA(x, cudaStreamSynchronize(x->c.stream), "sync");
+    harvest(x);
+    std::memset(out, 0, sizeof(*out));
+    out->ms_grid = x->ms[PH_GRID];
+    out->ms_octants = x->ms[PH_OCTANTS];
+    out->ms_select = x->ms[PH_SELECT];
+    out->ms_resolve = x->ms[PH_RESOLVE];
+    out->ms_hook = x->ms[PH_HOOK];
+    out->ms_flatten = x->ms[PH_FLATTEN];
+    out->launches = x->c.launches;
+    out->octant_launches = x->c.nns_launches;
+    out->rounds = x->c.round;
+    return EMST_OK;
+}
+
+emst_status emst_get_rescaled(emst_ctx* x, float* out, double* unit_x, int64_t cap)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (out) {
+        if (cap < c.n * c.dim) return set_err(x, EMST_EOVERFLOW, "buffer too small");
+        EMST_CUDA(x, cudaMemcpyAsync(out, c.scaled.p, sizeof(float) * c.n * c.dim, cudaMemcpyDeviceToHost, c.stream),
+                  "rescaled");
+    }
+    emst::NormParams np;
+    EMST_CUDA(x, cudaMemcpyAsync(&np, c.norm.p, sizeof(np), cudaMemcpyDeviceToHost, c.stream), "rescaled");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "rescaled");
+    if (unit_x) *unit_x = np.unitx;
+    return EMST_OK;
+}
+
+emst_status emst_solve(emst_ctx* x, const float* points, int64_t n, int dim, int32_t* uv, int64_t* n_edges,
+                       double* length)
+{
+    if (!x) return EMST_EINVAL;
+    emst_status st = do_initialize(x, points, n, dim, 0);
+    if (st != EMST_OK) return st;
+    if ((st = do_run(x)) != EMST_OK) return st;
+    int64_t ne = 0;
+    if ((st = emst_evaluate(x, &ne, length)) != EMST_OK) return st;
+    if (n_edges) *n_edges = ne;
+    if (uv) return emst_get_edges(x, uv, nullptr, n > 1 ? n - 1 : 0, nullptr);
+    return EMST_OK;
+}
+
+emst_status emst_solve_device(emst_ctx* x, const float* d_points, int64_t n, int dim, int32_t* d_uv,
+                              double* d_length, int64_t* n_edges)
+{
+    if (!x) return EMST_EINVAL;
+    emst_status st = do_initialize(x, d_points, n, dim, 1);
+    if (st != EMST_OK) return st;
+    if ((st = do_run(x)) != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (d_length) EMST_CUDA(x, emst::evaluate_length(c, d_length), "evaluate");
+    if (x->c.profile) {
+        EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+        harvest(x);
+    }
+    if (d_uv && c.n_edges)
+        EMST_CUDA(x, cudaMemcpyAsync(d_uv, c.edges.p, sizeof(int32_t) * 2 * c.n_edges, cudaMemcpyDeviceToDevice,
+                                     c.stream),
+                  "edges");
+    if (n_edges) *n_edges = c.n_edges;
+    return EMST_OK;
+}
+
+}  // extern "C"

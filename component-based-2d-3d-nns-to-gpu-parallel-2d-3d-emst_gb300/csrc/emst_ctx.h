@@ -1,0 +1,160 @@
+// emst_ctx.h -- host-side context of the EMST library and the launchers that
+// the C ABI (emst_capi.cu) drives.
+//
+// HBM layout (all arrays indexed by position in leaf order unless noted):
+//   in        n*dim float   caller's points, input order (original frame)
+//   scaled    n*dim float   rescaled points, input order
+//   sp        n float4      rescaled points in leaf (Morton) order, .w = input id
+//   perm      n uint32      leaf position -> input id
+//   nlo/nhi   2L float4     bounding boxes of the implicit leaf tree (heap order)
+//   nid       2L int4       per node: two smallest input ids and their leaf positions
+//   cand      n*K uint64    per point: region nearest neighbours, deduplicated and
+//                           sorted by (d2, input id); (d2 bits << 32) | leaf position
+//   cnt/cur   n uint8       list length / first entry not yet known to be inside
+//   zflag     n uint8       list holds a zero-distance entry (recompute next round)
+//   lab       n uint32      component root (leaf position) of every point
+//   par       n uint32      union-find parent, meaningful for roots
+//   ckey      n uint64      per root: (d2 bits << 32) | min input id of its best edge
+//   cmax      n uint64      per root: (max input id << 32) | winner leaf position
+//   selq      n uint32      per point: selected partner this round
+//   selkey    n uint64      per point: selected edge key this round
+//   act/roots/prov/zero     work lists (leaf positions)
+//   edges     2(n-1) int32  output edges (input ids, u < v); eround: round per edge
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace emst {
+
+// Device-side counters.  n_act / n_roots hold the CURRENT list sizes between
+// kernels; a kernel that rebuilds a list first has its input size copied to
+// the matching s_* slot (stream-ordered), then appends into the live counter.
+struct DevCounters {
+    uint32_t n_act;
+    uint32_t n_roots;
+    uint32_t n_prov;
+    uint32_t n_edges;
+    uint32_t n_zero_next;
+    uint32_t n_other;
+    uint32_t err;
+    uint32_t pos0;  // leaf position of input point 0
+    uint32_t s_act;
+    uint32_t s_roots;
+    uint32_t pad[6];
+};
+
+struct NormParams {
+    float pmin[3];
+    float pmax[3];
+    float uxf;       // float(unitX)
+    float qscale;    // Morton quantisation scale
+    double unitx;    // unitX as the reference computes it (double)
+    float smax[3];   // rescaled maxima
+    float pad;
+};
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;  // elements
+};
+
+struct Ctx {
+    int device = 0;
+    int max_rounds = 100;
+    int warps_per_block = 4;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    int64_t n = 0;
+    int dim = 0;
+    int K = 0;
+    int64_t nchunk = 0;
+    int64_t L = 0;  // leaf slots (power of two >= nchunk)
+
+    const float* in = nullptr;  // bound input (device)
+    DevBuf<float> in_own;
+    DevBuf<float> scaled;
+    DevBuf<float4> sp;
+    DevBuf<uint32_t> perm, perm_alt;
+    DevBuf<uint64_t> mkey, mkey_alt;
+    DevBuf<unsigned char> sort_tmp;
+    DevBuf<float> part;  // reduction partials
+    DevBuf<NormParams> norm;
+    DevBuf<float4> nlo, nhi;
+    DevBuf<int4> nid;  // per node: two smallest input ids + leaf positions
+
+    DevBuf<uint64_t> cand;
+    DevBuf<unsigned char> cnt, cur, zflag;
+    DevBuf<int32_t> tab_id;
+    DevBuf<float> tab_d2;
+    bool keep_table = false;
+
+    DevBuf<uint32_t> lab, par, selq;
+    DevBuf<uint64_t> ckey, cmax, selkey;
+    DevBuf<uint32_t> act, act2, roots, roots2, prov, zero, zero2;
+    uint32_t n_act = 0, n_roots = 0, n_zero = 0;
+    DevBuf<int32_t> edges, eround;
+    DevBuf<DevCounters> ctr;
+    DevCounters* hctr = nullptr;  // pinned mirror
+    DevBuf<double> lpart;
+    DevBuf<double> dlen;
+    double* hlen = nullptr;  // pinned
+
+    // launch accounting (hand-written kernels) and optional phase timing
+    int64_t launches = 0;
+    int64_t nns_launches = 0;
+    bool profile = false;
+
+    int round = 0;        // rounds started
+    int phase = 0;        // 0 = not initialised, 1 = initialised
+    bool finished = false;
+    bool octants_done = false;
+    uint32_t n_edges = 0;
+    std::vector<int64_t> cum_edges;
+};
+
+// grid.cu
+cudaError_t grid_build(Ctx& c);
+// nns.cu
+cudaError_t nns_full(Ctx& c);
+cudaError_t nns_recompute_zero(Ctx& c);
+// boruvka.cu
+cudaError_t boruvka_init(Ctx& c);
+cudaError_t boruvka_flatten(Ctx& c);
+cudaError_t boruvka_select(Ctx& c);
+cudaError_t boruvka_resolve(Ctx& c);
+cudaError_t boruvka_hook(Ctx& c);
+cudaError_t boruvka_count_other(Ctx& c);
+cudaError_t evaluate_length(Ctx& c, double* d_out);
+cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out);
+cudaError_t table_to_host_order(Ctx& c);
+
+template <typename T>
+cudaError_t ensure(DevBuf<T>& b, size_t n)
+{
+    if (b.cap >= n && b.p) return cudaSuccess;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = n < 1 ? 1 : n;
+    cudaError_t e = cudaMalloc(&b.p, want * sizeof(T));
+    if (e == cudaSuccess) b.cap = want;
+    return e;
+}
+
+template <typename T>
+void release(DevBuf<T>& b)
+{
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace emst

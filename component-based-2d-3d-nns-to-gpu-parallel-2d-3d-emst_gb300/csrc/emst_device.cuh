@@ -1,0 +1,159 @@
+// emst_device.cuh -- device-side arithmetic shared by the EMST kernels.
+//
+// The arithmetic here is the parity contract with the reference:
+//   * squared distance: the float dot product of the float difference,
+//     f = dx*dx; f += dy*dy; f += dz*dz (basic_components/include/Node.h:241-250),
+//     with the accumulating steps fused (fma) as the reference's GPU build
+//     contracts them; written with explicit _rn intrinsics so that no
+//     compiler contraction can change it;
+//   * regions: dominant axis (|d[dir]| >= max |d|) gives the face
+//     2*dir + (d[dir] < 0); slab bit j (other axes in increasing order) is 0
+//     for d >= 0 and 1 for d <= 0, so ties and zeros belong to several
+//     regions (emst_coalition/include/NodeEMST.h:1207-1232);
+//   * order between candidates of one query: (d2, original id), which is
+//     EMST_isInf (basic_components/include/macros_cuda.h:37) restricted to a
+//     fixed query point.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace emst {
+
+constexpr int kLeaf = 32;  // points per spatial leaf = one warp of queries
+constexpr uint64_t kNoKey = ~0ull;
+
+template <int D>
+struct Dim;
+template <>
+struct Dim<2> {
+    static constexpr int K = 8;
+    static constexpr int NSLAB = 2;
+};
+template <>
+struct Dim<3> {
+    static constexpr int K = 24;
+    static constexpr int NSLAB = 4;
+};
+
+// Squared distance between two points given their float differences.
+template <int D>
+__device__ __forceinline__ float d2_of(float dx, float dy, float dz)
+{
+    float r = __fmul_rn(dx, dx);
+    r = __fmaf_rn(dy, dy, r);
+    if (D == 3) r = __fmaf_rn(dz, dz, r);
+    return r;
+}
+
+// Region bit mask of a candidate at offset d = q - p (general path: ties and zeros).
+template <int D>
+__device__ __forceinline__ uint32_t region_mask(float dx, float dy, float dz)
+{
+    constexpr int NS = Dim<D>::NSLAB;
+    float a[3] = {fabsf(dx), fabsf(dy), fabsf(dz)};
+    float d[3] = {dx, dy, dz};
+    float m = fmaxf(a[0], a[1]);
+    if (D == 3) m = fmaxf(m, a[2]);
+    uint32_t mask = 0;
+#pragma unroll
+    for (int dir = 0; dir < D; ++dir) {
+        if (!(a[dir] >= m)) continue;
+        int face = 2 * dir + (d[dir] < 0.f ? 1 : 0);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+            bool ok = true;
+            int bit = 0;
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                if (i == dir) continue;
+                bool neg = (s >> bit) & 1;
+                ok = ok && (neg ? (d[i] <= 0.f) : (d[i] >= 0.f));
+                ++bit;
+            }
+            if (ok) mask |= 1u << (face * NS + s);
+        }
+    }
+    return mask;
+}
+
+// Fast path: the single region of a candidate with one dominant axis and no
+// zero component on the other axes; returns -1 when the general path is needed.
+template <int D>
+__device__ __forceinline__ int region_fast(float dx, float dy, float dz)
+{
+    float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    if (D == 2) {
+        if (ax > ay) {
+            if (dy == 0.f) return -1;
+            return (0 + (dx < 0.f)) * 2 + (dy < 0.f);
+        }
+        if (ay > ax) {
+            if (dx == 0.f) return -1;
+            return (2 + (dy < 0.f)) * 2 + (dx < 0.f);
+        }
+        return -1;
+    } else {
+        if (ax > ay && ax > az) {
+            if (dy == 0.f || dz == 0.f) return -1;
+            return (0 + (dx < 0.f)) * 4 + (dy < 0.f) + 2 * (dz < 0.f);
+        }
+        if (ay > ax && ay > az) {
+            if (dx == 0.f || dz == 0.f) return -1;
+            return (2 + (dy < 0.f)) * 4 + (dx < 0.f) + 2 * (dz < 0.f);
+        }
+        if (az > ax && az > ay) {
+            if (dx == 0.f || dy == 0.f) return -1;
+            return (4 + (dz < 0.f)) * 4 + (dx < 0.f) + 2 * (dy < 0.f);
+        }
+        return -1;
+    }
+}
+
+// Does the relative box [a, b] (b >= a componentwise) meet the cone of region r?
+// Exact on float offsets: a candidate's offset fl(q - p) lies in
+// [fl(lo - p), fl(hi - p)] whenever q lies in [lo, hi].
+template <int D>
+__device__ __forceinline__ bool cone_hits(int r, const float* a, const float* b)
+{
+    constexpr int NS = Dim<D>::NSLAB;
+    int face = r / NS, s = r % NS;
+    int dir = face >> 1;
+    bool negf = face & 1;
+    float t = negf ? -a[dir] : b[dir];
+    if (t < 0.f) return false;
+    int bit = 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        if (i == dir) continue;
+        bool neg = (s >> bit) & 1;
+        float lo = neg ? -b[i] : a[i];
+        float hi = neg ? -a[i] : b[i];
+        if (lo > t || hi < 0.f) return false;
+        ++bit;
+    }
+    return true;
+}
+
+// 64-bit Morton codes.
+__device__ __forceinline__ uint64_t spread2(uint32_t x)
+{
+    uint64_t v = x;
+    v = (v | (v << 16)) & 0x0000FFFF0000FFFFull;
+    v = (v | (v << 8)) & 0x00FF00FF00FF00FFull;
+    v = (v | (v << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    v = (v | (v << 2)) & 0x3333333333333333ull;
+    v = (v | (v << 1)) & 0x5555555555555555ull;
+    return v;
+}
+__device__ __forceinline__ uint64_t spread3(uint32_t x)
+{
+    uint64_t v = x & 0x1FFFFF;
+    v = (v | (v << 32)) & 0x1F00000000FFFFull;
+    v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+    v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+    v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+}  // namespace emst

@@ -1,0 +1,240 @@
+"""Python binding of libemst_gb300.so (the C ABI in include/emst.h).
+
+Mirrors the reference's operator surface (emst_coalition/include/EMSTOperators.h,
+driven by SolutionEMST::activate / run in emst_coalition/src/SolutionEMSTOperators.cu):
+    initialize -> [flatten, test_termination, compute_octants, find_next_closest,
+                   find_min_pair, connect_union]* -> evaluate / edges / labels
+plus the one-shot solve() / solve_device().  There is no CPU fallback: if the
+CUDA library is missing or no GPU is present, the calls raise.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libemst_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "emst.h")
+
+STATUS = {0: "EMST_OK", 1: "EMST_EINVAL", 2: "EMST_ENOMEM", 3: "EMST_EOVERFLOW", 4: "EMST_ENOCONVERGE",
+          5: "EMST_ECUDA", 6: "EMST_ESTATE"}
+K_OF_DIM = {2: 8, 3: 24}
+
+
+class EmstError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_rounds", ctypes.c_int), ("warps_per_block", ctypes.c_int),
+                ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+class Profile(ctypes.Structure):
+    _fields_ = [("ms_grid", ctypes.c_double), ("ms_octants", ctypes.c_double), ("ms_select", ctypes.c_double),
+                ("ms_resolve", ctypes.c_double), ("ms_hook", ctypes.c_double), ("ms_flatten", ctypes.c_double),
+                ("launches", ctypes.c_int64), ("octant_launches", ctypes.c_int64), ("rounds", ctypes.c_int64),
+                ("reserved", ctypes.c_int64 * 5)]
+
+
+def build(jobs=4):
+    """Compile the CUDA library in-tree for sm_103a (make -C <package>)."""
+    subprocess.run(["make", "-s", "-j%d" % jobs, "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def declared_symbols():
+    """Entry points declared in include/emst.h."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:emst_status|const char\*)\s+(emst_\w+)\s*\(", txt, re.M)))
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libemst_gb300.so is not built (run build() / __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        P, i64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+        sig = {
+            "emst_create": [P, P], "emst_destroy": [P], "emst_set_stream": [P, P],
+            "emst_initialize": [P, P, i64, I, I], "emst_compute_octants": [P], "emst_find_next_closest": [P],
+            "emst_find_min_pair": [P], "emst_connect_union": [P], "emst_flatten": [P],
+            "emst_test_termination": [P, P], "emst_activate": [P, P], "emst_run": [P],
+            "emst_evaluate": [P, P, P], "emst_get_edges": [P, P, P, i64, P], "emst_get_labels": [P, P, i64],
+            "emst_get_round_stats": [P, P, P, i64], "emst_get_region_table": [P, P, P, i64],
+            "emst_get_rescaled": [P, P, P, i64], "emst_solve": [P, P, i64, I, P, P, P],
+            "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = ctypes.c_int
+        L.emst_last_error.argtypes = [P]
+        L.emst_last_error.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Emst:
+    """One context = one CUDA stream on one device."""
+
+    def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False):
+        cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0)
+        h = ctypes.c_void_p()
+        st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise EmstError(st, "emst_create failed")
+        self.h = h
+        self.n = 0
+        self.dim = 0
+
+    def _chk(self, st):
+        if st != 0:
+            raise EmstError(st, lib().emst_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().emst_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        self._chk(lib().emst_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    # --- operators -------------------------------------------------------
+    def initialize(self, pts=None, device_ptr=None, n=None, dim=None):
+        if device_ptr is not None:
+            self._chk(lib().emst_initialize(self.h, ctypes.c_void_p(device_ptr), int(n), int(dim), 1))
+            self.n, self.dim = int(n), int(dim)
+        else:
+            pts = np.ascontiguousarray(pts, dtype=np.float32)
+            self._keep = pts
+            self._chk(lib().emst_initialize(self.h, _p(pts), pts.shape[0], pts.shape[1], 0))
+            self.n, self.dim = pts.shape
+        return self
+
+    def flatten(self):
+        self._chk(lib().emst_flatten(self.h))
+
+    def test_termination(self):
+        v = ctypes.c_int64()
+        self._chk(lib().emst_test_termination(self.h, ctypes.byref(v)))
+        return v.value
+
+    def compute_octants(self):
+        self._chk(lib().emst_compute_octants(self.h))
+
+    def find_next_closest(self):
+        self._chk(lib().emst_find_next_closest(self.h))
+
+    def find_min_pair(self):
+        self._chk(lib().emst_find_min_pair(self.h))
+
+    def connect_union(self):
+        self._chk(lib().emst_connect_union(self.h))
+
+    def activate(self):
+        m = ctypes.c_int()
+        self._chk(lib().emst_activate(self.h, ctypes.byref(m)))
+        return bool(m.value)
+
+    def run(self):
+        self._chk(lib().emst_run(self.h))
+
+    # --- results ---------------------------------------------------------
+    def evaluate(self):
+        ne, ln = ctypes.c_int64(), ctypes.c_double()
+        self._chk(lib().emst_evaluate(self.h, ctypes.byref(ne), ctypes.byref(ln)))
+        return ne.value, ln.value
+
+    def edges(self, with_rounds=False):
+        cap = max(self.n - 1, 1)
+        uv = np.zeros((cap, 2), np.int32)
+        rd = np.zeros(cap, np.int32)
+        ne = ctypes.c_int64()
+        self._chk(lib().emst_get_edges(self.h, _p(uv), _p(rd), cap, ctypes.byref(ne)))
+        if with_rounds:
+            return uv[: ne.value].copy(), rd[: ne.value].copy()
+        return uv[: ne.value].copy()
+
+    def labels(self):
+        out = np.zeros(self.n, np.int32)
+        self._chk(lib().emst_get_labels(self.h, _p(out), self.n))
+        return out
+
+    def round_stats(self):
+        r = ctypes.c_int64()
+        cum = np.zeros(128, np.int64)
+        self._chk(lib().emst_get_round_stats(self.h, ctypes.byref(r), _p(cum), 128))
+        return cum[: r.value].copy()
+
+    def region_table(self):
+        K = K_OF_DIM[self.dim]
+        ids = np.zeros((self.n, K), np.int32)
+        d2 = np.zeros((self.n, K), np.float32)
+        self._chk(lib().emst_get_region_table(self.h, _p(ids), _p(d2), self.n * K))
+        return ids, d2
+
+    def profile(self):
+        p = Profile()
+        self._chk(lib().emst_get_profile(self.h, ctypes.byref(p)))
+        return {k: getattr(p, k) for k, _ in Profile._fields_ if k != "reserved"}
+
+    def rescaled(self):
+        out = np.zeros((self.n, self.dim), np.float32)
+        ux = ctypes.c_double()
+        self._chk(lib().emst_get_rescaled(self.h, _p(out), ctypes.byref(ux), self.n * self.dim))
+        return out, ux.value
+
+    # --- one-shot --------------------------------------------------------
+    def solve(self, pts):
+        pts = np.ascontiguousarray(pts, dtype=np.float32)
+        n, dim = pts.shape
+        uv = np.zeros((max(n - 1, 1), 2), np.int32)
+        ne, ln = ctypes.c_int64(), ctypes.c_double()
+        self._chk(lib().emst_solve(self.h, _p(pts), n, dim, _p(uv), ctypes.byref(ne), ctypes.byref(ln)))
+        self.n, self.dim = n, dim
+        return uv[: ne.value].copy(), ln.value
+
+    def solve_into(self, pts, uv_out):
+        """Host arrays in and out, no allocation: pts (n, dim) float32, uv_out (n-1, 2) int32."""
+        ne, ln = ctypes.c_int64(), ctypes.c_double()
+        self._chk(lib().emst_solve(self.h, _p(pts), pts.shape[0], pts.shape[1], _p(uv_out), ctypes.byref(ne),
+                                   ctypes.byref(ln)))
+        self.n, self.dim = pts.shape
+        return ne.value, ln.value
+
+    def solve_device(self, d_points, n, dim, d_uv, d_length):
+        ne = ctypes.c_int64()
+        self._chk(lib().emst_solve_device(self.h, ctypes.c_void_p(d_points), int(n), int(dim), ctypes.c_void_p(d_uv),
+                                          ctypes.c_void_p(d_length), ctypes.byref(ne)))
+        self.n, self.dim = int(n), int(dim)
+        return ne.value
+
+
+def solve(pts, device=0):
+    with Emst(device=device) as e:
+        return e.solve(pts)

@@ -1,0 +1,186 @@
+/*
+ * emst.h -- C ABI of the GB300-native Boruvka 2D/3D EMST library.
+ *
+ * Drop-in for the reference's EMST operator path (emst_coalition): a caller
+ * that drove SolutionEMST / EMSTOperators can drive the same sequence of
+ * operators through these entry points (initialise -> per round: flatten,
+ * termination test, find-next-closest, find-min-pair, connect-and-union ->
+ * evaluate / links), or call emst_solve() for the whole loop.
+ *
+ * Conventions
+ *   - Points are float, array-of-structs, n * dim values (dim 2 or 3), in the
+ *     caller's original coordinates (the reference's Grid<PointE<Dim>>
+ *     adaptiveMapOriginal).  Point ids are 0-based input positions.
+ *   - Every entry point returns an emst_status; no exception crosses the ABI.
+ *     emst_last_error() gives a message for the last failure on a context.
+ *   - One context = one CUDA stream on one device.  A context is not
+ *     thread-safe; distinct contexts may be used concurrently.
+ *   - Device buffers are owned by the context and reused across calls.
+ *
+ * Reference citations are relative to the reference project root.
+ */
+#ifndef EMST_GB300_H
+#define EMST_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EMST_OK = 0,
+    EMST_EINVAL = 1,      /* bad argument (dim, n, null pointer, NaN / Inf coordinate) */
+    EMST_ENOMEM = 2,      /* device or host allocation failed */
+    EMST_EOVERFLOW = 3,   /* a size limit of the call was exceeded */
+    EMST_ENOCONVERGE = 4, /* round cap (100) or an iteration cap was hit */
+    EMST_ECUDA = 5,       /* CUDA runtime error (message in emst_last_error) */
+    EMST_ESTATE = 6       /* operator called out of order */
+} emst_status;
+
+typedef struct emst_ctx emst_ctx;
+
+typedef struct {
+    int device;          /* CUDA device ordinal */
+    int max_rounds;      /* Boruvka round cap; 0 = the reference's 100
+                            (SolutionEMSTOperators.cu:210) */
+    int warps_per_block; /* NNS launch shape; 0 = autotuned default */
+    int keep_region_table; /* != 0: keep the round-1 region table for
+                              emst_get_region_table (n * K * 8 bytes) */
+    int profile;           /* != 0: time every phase with CUDA events */
+    int reserved[7];
+} emst_config;
+
+/* Per-phase device times (ms, accumulated since emst_initialize) and kernel
+ * launch counts, as the reference's TspResultInfo per-phase timers
+ * (emst_coalition/include/EMSTOperators.h:54-70, SolutionEMSTOperators.cu:167-373). */
+typedef struct {
+    double ms_grid;     /* initialise: rescale + cell keys + sort + leaf tree */
+    double ms_octants;  /* compute_octants (static-pruning region table) */
+    double ms_select;   /* find_next_closest */
+    double ms_resolve;  /* find_min_pair */
+    double ms_hook;     /* connect_union */
+    double ms_flatten;  /* flatten */
+    int64_t launches;          /* kernels launched by the library */
+    int64_t octant_launches;   /* of which region-table kernels */
+    int64_t rounds;
+    int64_t reserved[5];
+} emst_profile;
+
+/* Context lifetime.  Replaces CalculateurEMST::initialize / the static
+ * SolutionEMST object (emst_coalition/src/CalculateurEMST.cu:52-169) without
+ * global state.  cfg may be NULL for defaults. */
+emst_status emst_create(const emst_config* cfg, emst_ctx** out);
+emst_status emst_destroy(emst_ctx* ctx);
+const char* emst_last_error(const emst_ctx* ctx);
+
+/* Bind the context's work to an existing CUDA stream (cudaStream_t passed as
+ * a void*); NULL restores the context's own stream. */
+emst_status emst_set_stream(emst_ctx* ctx, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Operator API (mirrors EMSTOperators, emst_coalition/include/EMSTOperators.h)
+ * ------------------------------------------------------------------------- */
+
+/* Upload / bind points, rescale them and build the spatial grid.
+ * Replaces SolutionEMST::initialize(NetLink&, pMin, pMax)
+ * (emst_coalition/src/SolutionEMST.cu:273-509: rescale :349-379, sizing
+ * :305-341, cell grid :427-482) together with K_initializeSpiralSearch
+ * (EMSTOperators.h:80-110, 1436-1446), K_initDisjointSet (:330-343) and
+ * K_clearLinks (:374-387).
+ * points_are_device != 0: `points` is a device pointer the caller keeps alive
+ * until the next emst_initialize / emst_destroy. */
+emst_status emst_initialize(emst_ctx* ctx, const float* points, int64_t n, int dim, int points_are_device);
+
+/* Static-pruning region table: for every point the nearest point of each of
+ * the K = 2D*2^(D-1) regions (8 in 2D, 24 in 3D).  Replaces K_computeOctants
+ * (EMSTOperators.h:1466-1476 -> NodeComputeOctantMD::computeOctants,
+ * NodeEMST.h:1018-1296).  On rounds > 1 only points whose table holds a
+ * zero-distance entry are recomputed, as the reference does (:1051-1077). */
+emst_status emst_compute_octants(emst_ctx* ctx);
+
+/* Per point: nearest table entry outside its component.  Replaces
+ * K_findNextClosestPoint (EMSTOperators.h:1490-1500 ->
+ * NodeComputeOctantMD::search, NodeEMST.h:1303-1384). */
+emst_status emst_find_next_closest(emst_ctx* ctx);
+
+/* Per component: shortest outgoing edge under the (d2, min id, max id)
+ * order.  Replaces K_createComponentList + K_findMinPair
+ * (NodeEMST.h:817-955). */
+emst_status emst_find_min_pair(emst_ctx* ctx);
+
+/* Hook components along their winning edges and append the edges.  Replaces
+ * K_connectComponentAndUnion (EMSTOperators.h:1267-1303, 1802-1814). */
+emst_status emst_connect_union(emst_ctx* ctx);
+
+/* Compress the disjoint-set forest so every point holds its root.  Replaces
+ * K_flatten_DST (EMSTOperators.h:412-433, 1586-1599). */
+emst_status emst_flatten(emst_ctx* ctx);
+
+/* Number of points whose root differs from point 0's root (0 = finished).
+ * Replaces EMSTOperators::testTermination (EMSTOperators.h:1517-1536). */
+emst_status emst_test_termination(emst_ctx* ctx, int64_t* n_other);
+
+/* One Boruvka round = flatten, termination test, compute_octants,
+ * find_next_closest, find_min_pair, connect_union.  *more = 0 once finished.
+ * Replaces SolutionEMST::activate (SolutionEMSTOperators.cu:156-422). */
+emst_status emst_activate(emst_ctx* ctx, int* more);
+
+/* All rounds until one component remains (or the round cap).  Replaces
+ * SolutionEMST::run (SolutionEMSTOperators.cu:145-153). */
+emst_status emst_run(emst_ctx* ctx);
+
+/* Tree size (edges) and length, the length in ORIGINAL coordinates as
+ * sum of sqrt(double(float squared distance)).  Replaces SolutionEMST::evaluate
+ * (SolutionEMST.cu:560-581 -> K_EMST_evaluate_ST, EMSTOperators.h:262-292). */
+emst_status emst_evaluate(emst_ctx* ctx, int64_t* n_edges, double* length);
+
+/* Copy results to host memory.
+ * uv: 2 * cap int32 (u < v, original point ids); round_of_edge: cap int32
+ * (1-based Boruvka round that added the edge; may be NULL).  Edges are in
+ * the order the rounds produced them.  Replaces the per-point adjacency
+ * BufferLink::operator<< / NeuralNetEMST::writeLinks (BufferLink.h:245-279,
+ * NeuralNetEMST.h:275-326). */
+emst_status emst_get_edges(emst_ctx* ctx, int32_t* uv, int32_t* round_of_edge, int64_t cap, int64_t* n_edges);
+
+/* Root point id per point (the disjointSetMap, NeuralNetEMST.h:59-79). */
+emst_status emst_get_labels(emst_ctx* ctx, int32_t* labels, int64_t cap);
+
+/* Number of rounds run so far, and cumulative edge count after each round
+ * (cap entries). */
+emst_status emst_get_round_stats(emst_ctx* ctx, int64_t* rounds, int64_t* cum_edges, int64_t cap);
+
+/* The round-1 region table: ids (original point ids, -1 = empty region) and
+ * squared distances in the rescaled frame, n * K entries each, in region
+ * order face * 2^(D-1) + slab (NodeEMST.h:966-972). */
+emst_status emst_get_region_table(emst_ctx* ctx, int32_t* ids, float* d2, int64_t cap);
+
+/* Phase times and launch counts since the last emst_initialize (phase times
+ * need emst_config.profile != 0). */
+emst_status emst_get_profile(emst_ctx* ctx, emst_profile* out);
+
+/* Rescaled coordinates (n * dim floats, input order) and unitX
+ * (SolutionEMST.cu:305-364). */
+emst_status emst_get_rescaled(emst_ctx* ctx, float* out, double* unit_x, int64_t cap);
+
+/* ---------------------------------------------------------------------------
+ * One-shot solvers
+ * ------------------------------------------------------------------------- */
+
+/* Host buffers in, host buffers out: initialize + run + evaluate + get_edges.
+ * The e2e path of CalculateurEMST::run (CalculateurEMST.cu:236-260). */
+emst_status emst_solve(emst_ctx* ctx, const float* points, int64_t n, int dim, int32_t* uv, int64_t* n_edges,
+                       double* length);
+
+/* Device buffers in and out (points n*dim floats; uv 2*(n-1) int32;
+ * length one double), no host synchronisation except the per-round
+ * termination read. */
+emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
+                              double* d_length, int64_t* n_edges);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMST_GB300_H */

@@ -1,0 +1,257 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Bit-exact for everything integer (edge sets, per-round edge counts, labels,
+region-table ids) and for the float values the reference computes in float
+(rescaled coordinates, region-table squared distances).  Tree lengths are
+doubles summed in a different order: relative tolerance 1e-9 against the
+oracle, and 6 significant digits against the reference's recorded traces.
+"""
+import numpy as np
+import pytest
+
+import emst_workloads as W
+import pyoracle as O
+from families import KINDS, family
+
+pytestmark = pytest.mark.gpu
+
+TRACED = [("pts2d_1000", 2), ("pts2d_3000", 2), ("pts2d_4000", 2), ("pts3d_1000", 3), ("pts3d_2000", 3),
+          ("pts3d_10000", 3)]
+
+
+def _canon(e):
+    return O.canon(np.asarray(e, np.int64))
+
+
+def _is_spanning_tree(n, edges):
+    if len(edges) != n - 1:
+        return False
+    par = np.arange(n)
+
+    def find(x):
+        while par[x] != x:
+            par[x] = par[par[x]]
+            x = par[x]
+        return x
+
+    for u, v in edges:
+        a, b = find(u), find(v)
+        if a == b:
+            return False
+        par[a] = b
+    return True
+
+
+def test_golden_3000_edges_labels_length(gpu_lib, fixtures):
+    pts = fixtures["pts2d_3000"]
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        uv = e.edges()
+        ne, length = e.evaluate()
+        labels = e.labels()
+        stats = e.round_stats()
+    assert ne == 2999
+    assert np.array_equal(_canon(uv), _canon(fixtures["outypu_edges"]))
+    assert np.array_equal(labels, fixtures["outypu_labels"])
+    assert list(stats) == [2058, 2724, 2931, 2983, 2996, 2999]
+    assert float("%.6g" % length) == 359222.0
+    assert length == pytest.approx(O.length(pts, uv.astype(np.int64)), rel=1e-9)
+
+
+@pytest.mark.parametrize("key,dim", TRACED)
+def test_golden_round_traces(gpu_lib, fixtures, traces, key, dim):
+    pts = fixtures[key]
+    n = len(pts)
+    trace = traces["%dd" % dim]["%drandomCity.%dd" % (n, dim)][0]
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        uv, rounds = e.edges(with_rounds=True)
+        stats = e.round_stats()
+    assert list(stats) == [row[1] for row in trace]
+    uv = uv.astype(np.int64)
+    for k, row in enumerate(trace):
+        sel = uv[rounds <= k + 1]
+        assert len(sel) == row[1]
+        assert float("%.6g" % O.length(pts, sel)) == pytest.approx(row[2], rel=1e-6)
+    sp, _, _, _ = O.rescale(pts)
+    r = O.emst(sp, "faithful")
+    assert np.array_equal(_canon(uv), _canon(r.edges))
+    # same edges added in the same rounds as the reference's algorithm
+    for k in range(1, r.rounds + 1):
+        assert np.array_equal(_canon(uv[rounds == k]), _canon(r.edges[r.edge_round == k]))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rescale_bit_exact(gpu_lib, dim):
+    pts = family("cluster", 5000, dim, 11) * np.float32(123.25) - np.float32(7.5)
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        got, ux = e.rescaled()
+    ref, rux, _, _ = O.rescale(pts)
+    assert ux == rux
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("kind", KINDS)
+def test_region_table_bit_exact(gpu_lib, kind, dim):
+    pts = family(kind, 4000, dim, 21)
+    with gpu_lib.Emst(keep_region_table=True) as e:
+        e.initialize(pts)
+        e.flatten()
+        e.compute_octants()
+        ids, d2 = e.region_table()
+    sp, _, _, _ = O.rescale(pts)
+    ti, td = O.region_table(sp, "brute")
+    assert np.array_equal(ids.astype(np.int64), ti)
+    assert np.array_equal(d2.view(np.uint32), td.view(np.uint32))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("n", [2, 3, 17, 33, 1000, 6000])
+def test_edge_set_and_rounds_vs_oracle(gpu_lib, kind, dim, n):
+    pts = family(kind, n, dim, 1000 + n)
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        uv, rounds = e.edges(with_rounds=True)
+        stats = e.round_stats()
+    sp, _, _, _ = O.rescale(pts)
+    r = O.emst(sp, "faithful")
+    assert np.array_equal(_canon(uv), _canon(r.edges))
+    assert list(stats) == [int(x) for x in r.round_edges]
+    if n <= 2000:
+        assert np.array_equal(_canon(uv), _canon(O.prim(sp)))
+
+
+def test_operator_sequence_equals_run(gpu_lib):
+    pts = family("cluster", 20000, 3, 5)
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        ref_edges = _canon(e.edges())
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        others = []
+        for _ in range(100):
+            e.flatten()
+            k = e.test_termination()
+            others.append(k)
+            if k == 0:
+                break
+            e.compute_octants()
+            e.find_next_closest()
+            e.find_min_pair()
+            e.connect_union()
+        assert others[-1] == 0 and all(o > 0 for o in others[:-1])
+        assert np.array_equal(_canon(e.edges()), ref_edges)
+        assert len(set(e.labels().tolist())) == 1
+
+
+def test_operator_order_is_checked(gpu_lib):
+    with gpu_lib.Emst() as e:
+        e.initialize(family("uniform", 100, 2, 1))
+        with pytest.raises(gpu_lib.EmstError) as ex:
+            e.find_next_closest()
+        assert ex.value.status == 6
+
+
+def test_single_point_and_pairs(gpu_lib):
+    with gpu_lib.Emst() as e:
+        uv, length = e.solve(np.array([[0.5, 0.5]], np.float32))
+        assert len(uv) == 0 and length == 0.0
+        uv, length = e.solve(np.array([[0.0, 0.0, 0.0], [1.0, 2.0, 2.0]], np.float32))
+        assert _canon(uv).tolist() == [[0, 1]] and length == pytest.approx(3.0)
+
+
+def test_all_identical_points(gpu_lib):
+    pts = np.full((777, 3), 0.25, np.float32)
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        uv = e.edges()
+        _, length = e.evaluate()
+    sp, _, _, _ = O.rescale(pts)
+    assert np.array_equal(_canon(uv), _canon(O.emst(sp, "faithful").edges))
+    assert length == 0.0
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_non_finite_input_is_rejected(gpu_lib, bad):
+    pts = family("uniform", 1000, 2, 3)
+    pts[17, 1] = bad
+    with gpu_lib.Emst() as e:
+        with pytest.raises(gpu_lib.EmstError) as ex:
+            e.solve(pts)
+        assert ex.value.status == 1
+
+
+def test_bad_dim_is_rejected(gpu_lib):
+    with gpu_lib.Emst() as e:
+        with pytest.raises(gpu_lib.EmstError) as ex:
+            e.solve(np.zeros((10, 4), np.float32))
+        assert ex.value.status == 1
+
+
+def test_device_entry_point_matches_host(gpu_lib):
+    torch = pytest.importorskip("torch")
+    pts = family("cluster", 50000, 3, 9)
+    with gpu_lib.Emst() as e:
+        uv_h, len_h = e.solve(pts)
+    d_pts = torch.from_numpy(pts).cuda()
+    d_uv = torch.zeros((len(pts) - 1, 2), dtype=torch.int32, device="cuda")
+    d_len = torch.zeros(1, dtype=torch.float64, device="cuda")
+    with gpu_lib.Emst() as e:
+        e.set_stream(torch.cuda.current_stream().cuda_stream)
+        ne = e.solve_device(d_pts.data_ptr(), len(pts), 3, d_uv.data_ptr(), d_len.data_ptr())
+        torch.cuda.synchronize()
+    assert ne == len(pts) - 1
+    assert np.array_equal(_canon(d_uv.cpu().numpy()), _canon(uv_h))
+    assert d_len.item() == pytest.approx(len_h, rel=1e-12)
+
+
+def test_repeat_runs_are_identical(gpu_lib):
+    """Union-find compression runs concurrently; repeated solves in one
+    context (buffers holding the previous solve's data) must agree exactly."""
+    pts = family("cluster", 6000, 3, 7000)
+    ref = None
+    with gpu_lib.Emst() as e:
+        for _ in range(200):
+            uv, length = e.solve(pts)
+            if ref is None:
+                ref = _canon(uv)
+            assert np.array_equal(_canon(uv), ref)
+    pts = family("dups", 30000, 2, 4)
+    outs = []
+    with gpu_lib.Emst() as e:
+        for _ in range(3):
+            uv, length = e.solve(pts)
+            outs.append((_canon(uv), length))
+    for uv, length in outs[1:]:
+        assert np.array_equal(uv, outs[0][0])
+        assert length == pytest.approx(outs[0][1], rel=1e-12)
+
+
+@pytest.mark.parametrize("name,n", [("gauss3d_1e6", 1_000_000), ("bezier2d_1e7", 1_000_000)])
+def test_full_size_structure(gpu_lib, name, n):
+    """Size-independent checks at workload scale: the GPU's region table rows
+    equal the oracle's exact rows on a random sample, and the GPU edge set is
+    the MST of the GPU's own candidate graph (Kruskal under the same order),
+    which is a spanning tree."""
+    pts = W.make(name, n)
+    with gpu_lib.Emst(keep_region_table=True) as e:
+        e.initialize(pts)
+        e.run()
+        uv = e.edges()
+        ids, d2 = e.region_table()
+        scaled, _ = e.rescaled()
+    assert _is_spanning_tree(len(pts), uv)
+    rows = np.random.default_rng(0).choice(len(pts), 1500, replace=False)
+    ti, td = O.region_rows(scaled, rows)
+    assert np.array_equal(ids[rows].astype(np.int64), ti)
+    assert np.array_equal(d2[rows].view(np.uint32), td.view(np.uint32))
+    mst = O.kruskal_table(ids, d2)
+    assert np.array_equal(_canon(mst), _canon(uv))
