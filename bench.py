@@ -226,6 +226,9 @@ def main():
         launches += prof["launches"]
         nns_launches += prof["octant_launches"]
         rounds = prof["rounds"]
+        search = {"leaf_visits_per_warp": prof["leaf_visits"] / max(prof["search_warps"], 1),
+                  "node_tests_per_warp": prof["node_tests"] / max(prof["search_warps"], 1),
+                  "candidates_per_query": prof["candidates"] / max(n, 1)}
         assert ne == n - 1
     torch.cuda.synchronize()
     barrier()
@@ -278,9 +281,7 @@ def main():
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
                         "d2h_bytes_per_step": int(8 * (n - 1) + 8)},
-                "gpu_launches": launches, "clocks": clocks,
-                "phase_ms_per_step": {k: v / args.steps for k, v in []}}
-        line.pop("phase_ms_per_step")
+                "gpu_launches": launches, "clocks": clocks, "search": search}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -235,6 +235,10 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
               "counters");
     c.launches = 0;
     c.nns_launches = 0;
+    if (c.profile) {
+        EMST_CUDA(x, emst::ensure(c.nstats, 4), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 4 * sizeof(unsigned long long), c.stream), "stats");
+    }
     for (double& v : x->ms) v = 0.0;
     {
         Timed t(x, PH_GRID);
@@ -315,6 +319,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.nlo);
     emst::release(c.nhi);
     emst::release(c.nid);
+    emst::release(c.nstats);
     emst::release(c.cand);
     emst::release(c.cnt);
     emst::release(c.cur);
@@ -514,6 +519,14 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     out->launches = x->c.launches;
     out->octant_launches = x->c.nns_launches;
     out->rounds = x->c.round;
+    if (x->c.profile && x->c.nstats.p) {
+        unsigned long long st[4];
+        EMST_CUDA(x, cudaMemcpy(st, x->c.nstats.p, sizeof(st), cudaMemcpyDeviceToHost), "stats");
+        out->leaf_visits = (int64_t)st[0];
+        out->node_tests = (int64_t)st[1];
+        out->candidates = (int64_t)st[2];
+        out->search_warps = (int64_t)st[3];
+    }
     return EMST_OK;
 }
 

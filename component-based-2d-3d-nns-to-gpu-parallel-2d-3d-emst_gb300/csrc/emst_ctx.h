@@ -109,6 +109,7 @@ struct Ctx {
     int64_t launches = 0;
     int64_t nns_launches = 0;
     bool profile = false;
+    DevBuf<unsigned long long> nstats;  // region search: leaf visits, node tests, candidates, warps
 
     int round = 0;        // rounds started
     int phase = 0;        // 0 = not initialised, 1 = initialised

@@ -78,34 +78,32 @@ __device__ __forceinline__ uint32_t region_mask(float dx, float dy, float dz)
 
 // Fast path: the single region of a candidate with one dominant axis and no
 // zero component on the other axes; returns -1 when the general path is needed.
+// Branch-free (lanes of a warp hold different queries, so a dominant-axis
+// if-chain would diverge); d = q - p never holds -0.0 (x - x = +0.0), so the
+// sign bit is exactly d < 0.
 template <int D>
 __device__ __forceinline__ int region_fast(float dx, float dy, float dz)
 {
-    float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    const int sx = __float_as_uint(dx) >> 31, sy = __float_as_uint(dy) >> 31;
     if (D == 2) {
-        if (ax > ay) {
-            if (dy == 0.f) return -1;
-            return (0 + (dx < 0.f)) * 2 + (dy < 0.f);
-        }
-        if (ay > ax) {
-            if (dx == 0.f) return -1;
-            return (2 + (dy < 0.f)) * 2 + (dx < 0.f);
-        }
-        return -1;
+        const bool gx = ax > ay, gy = ay > ax;
+        const bool ok = (gx && dy != 0.f) || (gy && dx != 0.f);
+        const int r = gx ? (sx * 2 + sy) : (4 + sy * 2 + sx);
+        return ok ? r : -1;
     } else {
-        if (ax > ay && ax > az) {
-            if (dy == 0.f || dz == 0.f) return -1;
-            return (0 + (dx < 0.f)) * 4 + (dy < 0.f) + 2 * (dz < 0.f);
-        }
-        if (ay > ax && ay > az) {
-            if (dx == 0.f || dz == 0.f) return -1;
-            return (2 + (dy < 0.f)) * 4 + (dx < 0.f) + 2 * (dz < 0.f);
-        }
-        if (az > ax && az > ay) {
-            if (dx == 0.f || dy == 0.f) return -1;
-            return (4 + (dz < 0.f)) * 4 + (dx < 0.f) + 2 * (dy < 0.f);
-        }
-        return -1;
+        const int sz = __float_as_uint(dz) >> 31;
+        const bool gx = ax > ay && ax > az;
+        const bool gy = ay > ax && ay > az;
+        const bool gz = az > ax && az > ay;
+        const bool nzx = dx != 0.f, nzy = dy != 0.f, nzz = dz != 0.f;
+        const bool ok = (gx && nzy && nzz) || (gy && nzx && nzz) || (gz && nzx && nzy);
+        // face * 4 + slab, slab bits over the other axes in increasing order
+        const int rx = sx * 4 + sy + 2 * sz;
+        const int ry = 8 + sy * 4 + sx + 2 * sz;
+        const int rz = 16 + sz * 4 + sx + 2 * sy;
+        const int r = gx ? rx : (gy ? ry : rz);
+        return ok ? r : -1;
     }
 }
 

@@ -36,13 +36,14 @@ namespace {
 constexpr int kStack = 64;
 constexpr unsigned kFull = 0xffffffffu;
 
-template <int D, int WPB>
+template <int D, int WPB, bool LIST>
 __global__ void __launch_bounds__(WPB * 32)
     k_nns(const float4* __restrict__ sp, const float4* __restrict__ nlo, const float4* __restrict__ nhi,
           const int4* __restrict__ nid, uint32_t n, uint32_t L, uint32_t nchunk, const uint32_t* __restrict__ qlist,
           uint32_t nq, const uint32_t* __restrict__ lab, uint64_t* __restrict__ cand, unsigned char* __restrict__ cnt,
           unsigned char* __restrict__ cur, unsigned char* __restrict__ zflag, uint32_t* __restrict__ zero_out,
-          uint32_t* __restrict__ zero_count, int32_t* __restrict__ tab_id, float* __restrict__ tab_d2)
+          uint32_t* __restrict__ zero_count, int32_t* __restrict__ tab_id, float* __restrict__ tab_d2,
+          unsigned long long* __restrict__ stats)
 {
     constexpr int K = Dim<D>::K;
     constexpr int NS = Dim<D>::NSLAB;
@@ -54,7 +55,7 @@ __global__ void __launch_bounds__(WPB * 32)
 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t task = blockIdx.x * WPB + w;
-    const bool listmode = qlist != nullptr;
+    constexpr bool listmode = LIST;
     if (listmode ? (uint64_t)task * 32 >= nq : task >= nchunk) return;  // warp-uniform
 
     uint32_t me;
@@ -85,6 +86,8 @@ __global__ void __launch_bounds__(WPB * 32)
         snap[r] = INFINITY;
     }
     float maxall = valid ? INFINITY : -1.f;
+    // search statistics (only accumulated when stats != nullptr)
+    uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
 
     auto refresh = [&]() {
         maxall = -1.f;
@@ -110,6 +113,7 @@ __global__ void __launch_bounds__(WPB * 32)
         const float dy = __fsub_rn(cy_, P.y);
         const float dz = __fsub_rn(cz_, P.z);
         const float d2 = d2_of<D>(dx, dy, dz);
+        if (d2 > maxall) return;  // cannot improve any region (all non-empty)
         if (listmode && d2 == 0.f && lab[sq] == labp) return;
         int r = region_fast<D>(dx, dy, dz);
         if (r >= 0) {
@@ -131,7 +135,9 @@ __global__ void __launch_bounds__(WPB * 32)
         if ((uint32_t)lane < m) t = sp[base + lane];
         s_tile[w][lane] = t;
         __syncwarp();
+        ++st_leaves;
         if (need) {
+            st_cands += m;
             for (uint32_t j = 0; j < m; ++j) {
                 const float4 c = s_tile[w][j];
                 const int oq = __float_as_int(c.w);
@@ -144,43 +150,59 @@ __global__ void __launch_bounds__(WPB * 32)
     };
 
     // May the box [lo, hi] hold a point that improves one of this lane's
-    // regions?  lb2 is a lower bound of d2 over the box computed with the same
-    // rounded operations as d2 (monotone, so lb2 <= d2 for every point
-    // inside); a region needs the box only if the box meets its cone
-    // (exact on the float offsets) and lb2 <= its current minimum.
+    // regions?  For region R (dominant axis dir with sign, slab signs on the
+    // other axes) every point q of box and cone has |d_i| >= L_i on the other
+    // axes (the box's distance from 0 on the slab's side) and
+    // |d_dir| >= T = max(L_dir, L_i) (dominance), so d2(q) >= d2_of(T, L_i)
+    // evaluated with the same rounded operations (monotone): an exact lower
+    // bound on the float offsets, compared with the region's minimum
+    // (<=, because an equal d2 with a smaller id still improves it).
     auto needs = [&](const float4& lo, const float4& hi) -> bool {
         if (!valid) return false;
-        const float ax = __fsub_rn(lo.x, P.x), ay = __fsub_rn(lo.y, P.y), az = __fsub_rn(lo.z, P.z);
-        const float bx = __fsub_rn(hi.x, P.x), by = __fsub_rn(hi.y, P.y), bz = __fsub_rn(hi.z, P.z);
-        const float gx = fmaxf(fmaxf(ax, -bx), 0.f);
-        const float gy = fmaxf(fmaxf(ay, -by), 0.f);
-        const float gz = D == 3 ? fmaxf(fmaxf(az, -bz), 0.f) : 0.f;
-        const float lb2 = d2_of<D>(gx, gy, gz);
-        if (lb2 > maxall) return false;
-        const float a[3] = {ax, ay, az};
-        const float b[3] = {bx, by, bz};
+        const float a[3] = {__fsub_rn(lo.x, P.x), __fsub_rn(lo.y, P.y), __fsub_rn(lo.z, P.z)};
+        const float b[3] = {__fsub_rn(hi.x, P.x), __fsub_rn(hi.y, P.y), __fsub_rn(hi.z, P.z)};
+        {
+            const float gx = fmaxf(fmaxf(a[0], -b[0]), 0.f);
+            const float gy = fmaxf(fmaxf(a[1], -b[1]), 0.f);
+            const float gz = D == 3 ? fmaxf(fmaxf(a[2], -b[2]), 0.f) : 0.f;
+            if (d2_of<D>(gx, gy, gz) > maxall) return false;
+        }
+        // per axis, per side: lower bound of |d| and feasibility
+        float Lp[3], Ln[3];
+        bool fp[3], fn[3];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            Lp[i] = fmaxf(a[i], 0.f);
+            Ln[i] = fmaxf(-b[i], 0.f);
+            fp[i] = b[i] >= 0.f;
+            fn[i] = a[i] <= 0.f;
+        }
         bool hit = false;
 #pragma unroll
         for (int f = 0; f < 2 * D; ++f) {
             const int dir = f >> 1;
-            const float t = (f & 1) ? -a[dir] : b[dir];
-            bool pos_ok[3], neg_ok[3];
-#pragma unroll
-            for (int i = 0; i < D; ++i) {
-                pos_ok[i] = a[i] <= t && b[i] >= 0.f;
-                neg_ok[i] = -b[i] <= t && a[i] <= 0.f;
-            }
+            const bool neg = f & 1;
+            const float Ld = neg ? Ln[dir] : Lp[dir];
+            const float Hd = neg ? -a[dir] : b[dir];
+            const bool fd = neg ? fn[dir] : fp[dir];
 #pragma unroll
             for (int s = 0; s < NS; ++s) {
-                bool ok = t >= 0.f;
+                float l[3] = {0.f, 0.f, 0.f};
+                float T = Ld;
+                bool ok = fd;
                 int bit = 0;
 #pragma unroll
                 for (int i = 0; i < D; ++i) {
                     if (i == dir) continue;
-                    ok = ok && (((s >> bit) & 1) ? neg_ok[i] : pos_ok[i]);
+                    const bool sn = (s >> bit) & 1;
+                    l[i] = sn ? Ln[i] : Lp[i];
+                    ok = ok && (sn ? fn[i] : fp[i]);
+                    T = fmaxf(T, l[i]);
                     ++bit;
                 }
-                hit |= ok && snap[f * NS + s] >= lb2;
+                l[dir] = T;
+                ok = ok && T <= Hd;
+                hit |= ok && d2_of<D>(l[0], l[1], l[2]) <= snap[f * NS + s];
             }
         }
         return hit;
@@ -210,6 +232,7 @@ __global__ void __launch_bounds__(WPB * 32)
         if (node == own) continue;
         const float4 lo = nlo[node], hi = nhi[node];
         if (lo.x > hi.x) continue;
+        ++st_nodes;
         const bool need = needs(lo, hi);
         if (!__any_sync(kFull, need)) continue;
         if (lo.x == hi.x && lo.y == hi.y && lo.z == hi.z) {
@@ -245,6 +268,16 @@ __global__ void __launch_bounds__(WPB * 32)
         }
     }
 
+    if (stats) {
+        unsigned long long cands = st_cands;
+        for (int o = 16; o > 0; o >>= 1) cands += __shfl_xor_sync(kFull, cands, o);
+        if (lane == 0) {
+            atomicAdd(&stats[0], (unsigned long long)st_leaves);
+            atomicAdd(&stats[1], (unsigned long long)st_nodes);
+            atomicAdd(&stats[2], cands);
+            atomicAdd(&stats[3], 1ull);
+        }
+    }
     if (!valid) return;
     // Region-order table (round 1 only; optional).
     if (tab_id) {
@@ -303,10 +336,11 @@ cudaError_t launch(Ctx& c, const uint32_t* qlist, uint32_t nq, uint32_t* zero_ou
     unsigned tasks = qlist ? (unsigned)((nq + 31) / 32) : (unsigned)c.nchunk;
     if (tasks == 0) return cudaSuccess;
     unsigned blocks = (tasks + WPB - 1) / WPB;
-    k_nns<D, WPB><<<blocks, WPB * 32, 0, c.stream>>>(
+    auto kern = qlist ? k_nns<D, WPB, true> : k_nns<D, WPB, false>;
+    kern<<<blocks, WPB * 32, 0, c.stream>>>(
         c.sp.p, c.nlo.p, c.nhi.p, c.nid.p, (uint32_t)c.n, (uint32_t)c.L, (uint32_t)c.nchunk, qlist, nq,
         qlist ? c.lab.p : nullptr, c.cand.p, c.cnt.p, c.cur.p, c.zflag.p, zero_out, zero_count,
-        table ? c.tab_id.p : nullptr, table ? c.tab_d2.p : nullptr);
+        table ? c.tab_id.p : nullptr, table ? c.tab_d2.p : nullptr, c.profile ? c.nstats.p : nullptr);
     c.launches++;
     c.nns_launches++;
     return cudaGetLastError();

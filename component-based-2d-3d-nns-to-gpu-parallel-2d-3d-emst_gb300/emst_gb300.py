@@ -38,7 +38,8 @@ class Profile(ctypes.Structure):
     _fields_ = [("ms_grid", ctypes.c_double), ("ms_octants", ctypes.c_double), ("ms_select", ctypes.c_double),
                 ("ms_resolve", ctypes.c_double), ("ms_hook", ctypes.c_double), ("ms_flatten", ctypes.c_double),
                 ("launches", ctypes.c_int64), ("octant_launches", ctypes.c_int64), ("rounds", ctypes.c_int64),
-                ("reserved", ctypes.c_int64 * 5)]
+                ("leaf_visits", ctypes.c_int64), ("node_tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
+                ("search_warps", ctypes.c_int64), ("reserved", ctypes.c_int64 * 1)]
 
 
 def build(jobs=4):

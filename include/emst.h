@@ -65,7 +65,14 @@ typedef struct {
     int64_t launches;          /* kernels launched by the library */
     int64_t octant_launches;   /* of which region-table kernels */
     int64_t rounds;
-    int64_t reserved[5];
+    /* region search work (static pruning), all launches: leaves (32-point
+     * cells) visited per warp, tree nodes tested, candidate points folded
+     * (summed over queries), warps (one per 32 queries) */
+    int64_t leaf_visits;
+    int64_t node_tests;
+    int64_t candidates;
+    int64_t search_warps;
+    int64_t reserved[1];
 } emst_profile;
 
 /* Context lifetime.  Replaces CalculateurEMST::initialize / the static
