@@ -73,6 +73,7 @@ def lib():
             "emst_get_round_stats": [P, P, P, i64], "emst_get_region_table": [P, P, P, i64],
             "emst_get_rescaled": [P, P, P, i64], "emst_solve": [P, P, i64, I, P, P, P],
             "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
+            "emst_region_table_noalloc": [P, i64, I, P, P, P],
         }
         for name, args in sig.items():
             f = getattr(L, name)

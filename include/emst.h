@@ -186,6 +186,34 @@ emst_status emst_solve(emst_ctx* ctx, const float* points, int64_t n, int dim, i
 emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
                               double* d_length, int64_t* n_edges);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free region table
+ * ------------------------------------------------------------------------- */
+
+/* Largest point set emst_region_table_noalloc accepts, and the size of the
+ * device array it works in (held by every GPU that loads the library until
+ * the process exits). */
+#define EMST_NOALLOC_MAX_POINTS 32768
+#define EMST_NOALLOC_SCRATCH_BYTES (12u << 20)
+
+/* No counterpart in the reference.  The same region table as
+ * emst_compute_octants + emst_get_region_table (ids as input point ids, -1 for
+ * an empty region, and squared distances in the rescaled frame, n * K entries
+ * each), for callers that must not allocate device memory once they are
+ * running: a host whose device memory is owned by its own allocator, a
+ * real-time pipeline where a cudaMalloc / cudaFree may stall or fail mid-run,
+ * or a plugin whose processing callback forbids allocation.  The caller passes
+ * device buffers for the points (n * dim floats) and both outputs; every
+ * intermediate buffer lives in one fixed device array inside the library, so
+ * nothing is allocated and n is limited to EMST_NOALLOC_MAX_POINTS (larger n
+ * returns EMST_EOVERFLOW).  The first call on a device looks up that array's
+ * device address (make it before any stream capture).  Calls share the array:
+ * calls that may overlap on the GPU race and must be serialised by the caller.
+ * Synchronises `stream` (a cudaStream_t, NULL = legacy default stream) before
+ * returning; EMST_EINVAL for a non-finite coordinate. */
+emst_status emst_region_table_noalloc(const float* d_points, int64_t n, int dim, int32_t* d_ids, float* d_d2,
+                                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif
