@@ -96,10 +96,17 @@ class ClockSampler:
 
 
 def nns_bytes(n, dim):
-    """Algorithmic bytes of one region-table launch: read the sorted points once
-    (4*D per point) and write K (id, d2) pairs (8*K per point)."""
+    """Algorithmic bytes of one static region-table launch (k_nns): read the
+    sorted points once (4*D per point) and write K (id, d2) pairs (8*K per point)."""
     K = 8 if dim == 2 else 24
     return n * (4 * dim + 8 * K)
+
+
+CNNS_BYTES_PER_QUERY = 16 + 4 + 12 + 8
+"""Algorithmic bytes per query of the component search (k_cnns): read the
+query point (float4) and its label, write partner + key, one 8-byte atomicMin."""
+
+PHASES = ["ms_grid", "ms_octants", "ms_select", "ms_resolve", "ms_hook", "ms_flatten"]
 
 
 def traffic_from_profile(name, n):
@@ -166,6 +173,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=100_000)
     ap.add_argument("--ref-sample", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", type=int, default=0, help="0: component search, 1: static region table")
+    ap.add_argument("--no-static", action="store_true", help="skip the one-step static-table comparison")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -194,7 +203,7 @@ def main():
     d_len = torch.empty(1, dtype=torch.float64, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
-    ctx = E.Emst(device=local, profile=True)
+    ctx = E.Emst(device=local, profile=True, search_mode=args.mode)
     ctx.set_stream(stream.cuda_stream)
 
     def step():
@@ -212,7 +221,10 @@ def main():
     sampler.start()
     barrier()
     torch.cuda.synchronize()
-    dev_ms, nns_ms, launches, nns_launches, rounds = [], 0.0, 0, 0, 0
+    dev_ms, launches, rounds = [], 0, 0
+    phase = {k: 0.0 for k in PHASES}
+    stat = {"leaf_visits": 0, "node_tests": 0, "candidates": 0, "search_warps": 0, "search_queries": 0,
+            "octant_launches": 0}
     for _ in range(args.steps):
         flush.zero_()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -222,13 +234,12 @@ def main():
         ev1.synchronize()
         dev_ms.append(ev0.elapsed_time(ev1))
         prof = ctx.profile()
-        nns_ms += prof["ms_octants"]
+        for k in PHASES:
+            phase[k] += prof[k]
+        for k in stat:
+            stat[k] += prof[k]
         launches += prof["launches"]
-        nns_launches += prof["octant_launches"]
         rounds = prof["rounds"]
-        search = {"leaf_visits_per_warp": prof["leaf_visits"] / max(prof["search_warps"], 1),
-                  "node_tests_per_warp": prof["node_tests"] / max(prof["search_warps"], 1),
-                  "candidates_per_query": prof["candidates"] / max(n, 1)}
         assert ne == n - 1
     torch.cuda.synchronize()
     barrier()
@@ -255,10 +266,38 @@ def main():
     e2e = world * n * args.steps / e2e_s / 1e6
 
     peak, peak_kind = peaks()
-    per_launch_ms = nns_ms / max(nns_launches, 1)
-    alg = nns_bytes(n, dim)
+    K = args.steps
+    if args.mode in (0, 2):
+        kernel = "k_cnns_t" if args.mode == 0 else "k_cnns"
+        n_launch = max(stat["octant_launches"], 1)
+        per_launch_ms = phase["ms_select"] / n_launch
+        alg = CNNS_BYTES_PER_QUERY * stat["search_queries"] / n_launch
+    else:
+        kernel = "k_nns"
+        n_launch = max(stat["octant_launches"], 1)
+        per_launch_ms = phase["ms_octants"] / n_launch
+        alg = nns_bytes(n, dim) * K / n_launch
     achieved = alg / (per_launch_ms / 1e3) / 1e9
-    traffic = traffic_from_profile(args.workload, n)
+    traffic = traffic_from_profile("%s_%s" % (kernel, args.workload), n)
+    search = {"leaf_visits_per_warp": stat["leaf_visits"] / max(stat["search_warps"], 1),
+              "node_tests_per_warp": stat["node_tests"] / max(stat["search_warps"], 1),
+              "candidates_per_point": stat["candidates"] / (n * K),
+              "searches_per_point": stat["search_queries"] / (n * K) if args.mode != 1 else 1.0}
+    phase_ms = {k[3:]: round(v / K, 3) for k, v in phase.items()}
+
+    static = None
+    if args.mode != 1 and not args.no_static:
+        with E.Emst(device=local, search_mode=1) as cs:
+            cs.set_stream(stream.cuda_stream)
+            cs.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cs.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            static = {"value": n / (e0.elapsed_time(e1) / 1e3) / 1e6, "unit": "Mpoints/s", "steps": 1,
+                      "note": "static-pruning region table (the reference's computeOctants), same edge set"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -272,12 +311,15 @@ def main():
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": args.workload, "n": n, "dim": dim, "rounds": rounds,
+                           "search": {0: "component, thread per query", 1: "static region table",
+                                      2: "component, warp per 32 queries"}[args.mode],
                            "l2": "512 MB buffer written between timed steps; working set > 129 MB L2",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic, "kernel": "k_nns",
+                             "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                              "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
                              "peak_kind": peak_kind},
+                "phase_ms": phase_ms, "static_table_mode": static,
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
                         "d2h_bytes_per_step": int(8 * (n - 1) + 8)},

@@ -214,8 +214,8 @@ __global__ void k_relabel(uint32_t n, uint32_t* __restrict__ lab, const uint32_t
 
 __global__ void k_compact_roots(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
                                 const uint32_t* __restrict__ par, uint64_t* __restrict__ ckey,
-                                uint64_t* __restrict__ cmax, uint32_t* __restrict__ roots_next,
-                                uint32_t* __restrict__ n_roots_next)
+                                uint64_t* __restrict__ cmax, uint32_t* __restrict__ clb,
+                                uint32_t* __restrict__ roots_next, uint32_t* __restrict__ n_roots_next)
 {
     const uint32_t total = *n_roots;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
@@ -228,6 +228,7 @@ __global__ void k_compact_roots(const uint32_t* __restrict__ roots, const uint32
             if (keep) {
                 ckey[c] = kNoKey;
                 cmax[c] = kNoKey;
+                if (clb) clb[c] = 0x7f800000u;  // +inf
             }
         }
         warp_append(keep, c, roots_next, n_roots_next);
@@ -327,7 +328,8 @@ cudaError_t boruvka_flatten(Ctx& c)
     cudaMemcpyAsync(&d->s_roots, &d->n_roots, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream);
     cudaMemsetAsync(&d->n_roots, 0, sizeof(uint32_t), c.stream);
     k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->s_roots, c.par.p, c.ckey.p, c.cmax.p,
-                                                                c.roots2.p, &d->n_roots);
+                                                                c.search_mode == 0 ? c.clb.p : nullptr, c.roots2.p,
+                                                                &d->n_roots);
     std::swap(c.roots.p, c.roots2.p);
     c.launches += 3;
     return cudaGetLastError();

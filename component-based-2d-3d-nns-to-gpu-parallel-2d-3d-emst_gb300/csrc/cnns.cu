@@ -1,0 +1,553 @@
+// cnns.cu -- component nearest-neighbour search (the default solver mode).
+//
+// Each Boruvka round needs, per component, its shortest outgoing edge under
+// the order (d2, min id, max id) (EMST_isInf, macros_cuda.h:37).  The
+// reference reaches it through a static region table (NodeEMST.h:1018-1384);
+// this mode searches for it directly, per point, in the same leaf tree:
+//
+//   * node labels: after the labels are flattened, every tree node records
+//     the component all its points share (or MIXED); a point's search skips
+//     subtrees of its own component entirely;
+//   * shared bound: a point prunes with min(its own best, the best key its
+//     component holds so far in the 64-bit atomicMin slot) -- the slot is an
+//     upper bound of the component's minimum, so the minimum is never pruned;
+//   * reuse: a point whose previous partner is still outside its component
+//     keeps it (the outside set only shrinks, so the minimum stands); only
+//     the others ("dirty" points) search.  A result is kept for reuse only if
+//     the shared bound did not cut the search short of it;
+//   * lower bounds: every search leaves lbp[p] <= d2 of p's nearest point
+//     outside its component, which stays valid in later rounds (components
+//     only grow).  Dirty points search in two passes: first those with the
+//     smallest bounds in their component (likely to hold its minimum), then
+//     the rest, each skipped outright when its bound exceeds the best key its
+//     component already holds (it cannot hold the minimum).
+//
+// For a fixed query the candidate order is (d2, input id), which is the
+// reference order restricted to that query, so each component's minimum --
+// and with it every round's edge set -- equals the static-table method's.
+#include <climits>
+
+#include "emst_ctx.h"
+#include "emst_device.cuh"
+
+namespace emst {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kMixed = 0xffffffffu;
+constexpr uint32_t kEmpty = 0xfffffffeu;
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kStack = 64;
+constexpr int kLeavesPerBlock = 1024;
+
+__device__ __forceinline__ uint32_t merge_label(uint32_t a, uint32_t b)
+{
+    if (a == kEmpty) return b;
+    if (b == kEmpty) return a;
+    return a == b ? a : kMixed;
+}
+
+// Leaves of one block (a subtree of kLeavesPerBlock leaf slots, or all of L
+// when smaller) and the levels above them inside that subtree.
+__global__ void __launch_bounds__(1024)
+    k_node_labels_sub(const uint32_t* __restrict__ lab, uint32_t n, uint32_t nchunk, uint32_t L, uint32_t span,
+                      uint32_t* __restrict__ nlab)
+{
+    __shared__ uint32_t s[kLeavesPerBlock];
+    const uint32_t first = blockIdx.x * span;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t l = w; l < span; l += blockDim.x >> 5) {
+        const uint32_t c = first + l;
+        uint32_t out = kEmpty;
+        if (c < nchunk) {
+            const uint32_t j = c * 32 + lane;
+            const bool v = j < n;
+            const uint32_t my = v ? lab[j] : 0u;
+            const uint32_t l0 = __shfl_sync(kFull, my, 0);
+            out = __all_sync(kFull, !v || my == l0) ? l0 : kMixed;
+        }
+        if (lane == 0) {
+            s[l] = out;
+            nlab[L + c] = out;
+        }
+    }
+    __syncthreads();
+    uint32_t base = (L + first);
+    for (uint32_t cnt = span >> 1; cnt >= 1; cnt >>= 1) {
+        base >>= 1;
+        uint32_t v = 0;
+        const bool act = threadIdx.x < cnt;
+        if (act) v = merge_label(s[2 * threadIdx.x], s[2 * threadIdx.x + 1]);
+        __syncthreads();
+        if (act) {
+            s[threadIdx.x] = v;
+            nlab[base + threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// Levels above the per-block subtrees (nodes [1, top)), one block.
+__global__ void __launch_bounds__(1024) k_node_labels_top(uint32_t top, uint32_t* __restrict__ nlab)
+{
+    for (uint32_t h = top >> 1; h >= 1; h >>= 1) {
+        for (uint32_t t = threadIdx.x; t < h; t += blockDim.x)
+            nlab[h + t] = merge_label(nlab[2 * (h + t)], nlab[2 * (h + t) + 1]);
+        __syncthreads();
+    }
+}
+
+// Warp-aggregated append of `val` to list[] through counter *cnt.
+__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* list, uint32_t* cnt)
+{
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (uint32_t)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+// Points whose previous partner is still outside their component re-submit
+// it; the others go to the dirty list and fold their lower bound into their
+// component's minimum bound clb.
+__global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, const uint32_t* __restrict__ selq,
+                        const uint64_t* __restrict__ selkey, const float* __restrict__ lbp,
+                        uint64_t* __restrict__ ckey, uint32_t* __restrict__ clb, uint32_t* __restrict__ dirty,
+                        uint32_t* __restrict__ n_dirty, uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov)
+{
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t p = base + threadIdx.x;
+        bool is_dirty = false, record = false;
+        if (p < n) {
+            const uint32_t q = selq[p];
+            const uint32_t lp = lab[p];
+            if (q != kNone && lab[q] != lp) {
+                const uint64_t key = selkey[p];
+                if (key <= __ldcg(&ckey[lp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[lp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                is_dirty = true;
+                const uint32_t lb = __float_as_uint(lbp[p]);
+                if (lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
+            }
+        }
+        warp_append(is_dirty, p, dirty, n_dirty);
+        warp_append(record, p, prov, n_prov);
+    }
+}
+
+// One warp per 32 dirty points: nearest point outside the query's component.
+template <int D, int WPB>
+__global__ void __launch_bounds__(WPB * 32)
+    k_cnns(const float4* __restrict__ sp, const float4* __restrict__ nlo, const float4* __restrict__ nhi,
+           const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L, const uint32_t* __restrict__ dirty,
+           const uint32_t* __restrict__ n_dirty, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
+           uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
+           uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
+           uint32_t* __restrict__ defer, uint32_t* __restrict__ n_defer, unsigned long long* __restrict__ stats)
+{
+    __shared__ float4 s_tile[WPB][32];
+    __shared__ uint32_t s_tlab[WPB][32];
+    __shared__ uint32_t s_stack[WPB][kStack];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t total = *n_dirty;
+
+    for (uint32_t task = blockIdx.x * WPB + w; (uint64_t)task * 32 < total; task += gridDim.x * WPB) {
+        const uint32_t qi = task * 32 + lane;
+        const bool listed = qi < total;
+        const uint32_t me = listed ? dirty[qi] : 0u;
+        const uint32_t labp0 = listed ? lab[me] : kEmpty;
+        const float lb0 = listed ? lbp[me] : 0.f;
+        bool valid = listed, deferred = false;
+        if (listed) {
+            const uint64_t k = __ldcg(&ckey[labp0]);
+            const float cb0 = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+            if (lb0 > cb0) {
+                valid = false;  // cannot hold its component's minimum this round
+            } else if (pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp0]))) {
+                valid = false;  // not among its component's most promising points: second pass
+                deferred = true;
+            }
+        }
+        warp_append(deferred, me, defer, n_defer);
+        const float4 P = valid ? sp[me] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int op = __float_as_int(P.w);
+        const uint32_t labp = valid ? labp0 : kEmpty;
+
+        float bd = INFINITY;  // best d2
+        int bo = INT_MAX;     // its input id
+        int bs = -1;          // its leaf position
+        float cut = INFINITY; // smallest lower bound pruned only because of the shared bound
+        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
+        const uint32_t st_queries = __popc(__ballot_sync(kFull, valid));
+
+        auto shared_bound = [&]() -> float {
+            if (!valid) return -1.f;
+            const uint64_t k = __ldcg(&ckey[labp]);
+            return k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+        };
+        float cb = shared_bound();
+
+        // Is the node worth opening for this lane?  lb2 <= d2(q) for every
+        // point q in the box (same rounded operations, monotone).
+        auto needs = [&](uint32_t node, const float4& lo, const float4& hi) -> bool {
+            if (!valid) return false;
+            if (nlab[node] == labp) return false;  // all points in the query's component
+            const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+            const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+            const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+            const float lb2 = d2_of<D>(gx, gy, gz);
+            if (lb2 > bd) return false;
+            if (lb2 > cb) {
+                cut = fminf(cut, lb2);
+                return false;
+            }
+            return true;
+        };
+
+        const float cx = __shfl_sync(kFull, P.x, 0), cy = __shfl_sync(kFull, P.y, 0),
+                    cz = __shfl_sync(kFull, P.z, 0);
+        auto box_d2 = [&](uint32_t node) -> float {
+            const float4 lo = nlo[node], hi = nhi[node];
+            if (lo.x > hi.x) return INFINITY;
+            const float gx = fmaxf(fmaxf(lo.x - cx, cx - hi.x), 0.f);
+            const float gy = fmaxf(fmaxf(lo.y - cy, cy - hi.y), 0.f);
+            const float gz = fmaxf(fmaxf(lo.z - cz, cz - hi.z), 0.f);
+            return gx * gx + gy * gy + gz * gz;
+        };
+
+        int top = 0;
+        if (lane == 0) s_stack[w][0] = 1u;
+        top = 1;
+        __syncwarp();
+        while (top > 0) {
+            const uint32_t node = s_stack[w][--top];
+            __syncwarp();
+            const float4 lo = nlo[node], hi = nhi[node];
+            if (lo.x > hi.x) continue;
+            ++st_nodes;
+            const bool need = needs(node, lo, hi);
+            if (!__any_sync(kFull, need)) continue;
+            if (node >= L) {
+                const uint32_t base = (node - L) * 32;
+                const uint32_t m = min(32u, n - base);
+                float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+                uint32_t tl = kEmpty;
+                if ((uint32_t)lane < m) {
+                    t = sp[base + lane];
+                    tl = lab[base + lane];
+                }
+                s_tile[w][lane] = t;
+                s_tlab[w][lane] = tl;
+                __syncwarp();
+                ++st_leaves;
+                if (need) {
+                    st_cands += m;
+                    for (uint32_t j = 0; j < m; ++j) {
+                        if (s_tlab[w][j] == labp) continue;
+                        const float4 c = s_tile[w][j];
+                        const float dx = __fsub_rn(c.x, P.x);
+                        const float dy = __fsub_rn(c.y, P.y);
+                        const float dz = __fsub_rn(c.z, P.z);
+                        const float d2 = d2_of<D>(dx, dy, dz);
+                        const int oq = __float_as_int(c.w);
+                        if (d2 < bd || (d2 == bd && oq < bo)) {
+                            bd = d2;
+                            bo = oq;
+                            bs = (int)(base + j);
+                        }
+                    }
+                    cb = shared_bound();
+                }
+                __syncwarp();
+            } else {
+                const uint32_t c0 = 2 * node, c1 = 2 * node + 1;
+                const float d0 = box_d2(c0), d1 = box_d2(c1);
+                const uint32_t nearc = d0 <= d1 ? c0 : c1, farc = d0 <= d1 ? c1 : c0;
+                if (top + 2 > kStack) break;  // cannot happen for trees of depth < 62
+                if (lane == 0) {
+                    s_stack[w][top] = farc;
+                    s_stack[w][top + 1] = nearc;
+                }
+                top += 2;
+                __syncwarp();
+            }
+        }
+
+        bool record = false;
+        if (valid) {
+            // nothing closer than min(cut, bd) lies outside the component
+            const bool exact = bs >= 0 && bd < cut;
+            lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
+            if (bs >= 0) {
+                const uint32_t mn = (uint32_t)min(op, bo);
+                const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
+                // keep for reuse only if nothing cut off could still be as close
+                selq[me] = exact ? (uint32_t)bs : kNone;
+                selkey[me] = key;
+                if (key <= __ldcg(&ckey[labp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                selq[me] = kNone;
+            }
+        }
+        warp_append(record, me, prov, n_prov);
+        if (stats) {
+            unsigned long long cands = st_cands;
+            for (int o = 16; o > 0; o >>= 1) cands += __shfl_xor_sync(kFull, cands, o);
+            if (lane == 0) {
+                atomicAdd(&stats[0], (unsigned long long)st_leaves);
+                atomicAdd(&stats[1], (unsigned long long)st_nodes);
+                atomicAdd(&stats[2], cands);
+                atomicAdd(&stats[3], 1ull);
+                atomicAdd(&stats[4], (unsigned long long)st_queries);
+            }
+        }
+    }
+}
+
+// One thread per dirty point, each with its own traversal order: its own
+// leaf first, then a depth-first walk from the root pushing the nearer child
+// last, so every query sees good bounds early (queries of later rounds are
+// sparse, and one warp-wide order would serve only some of them).
+template <int D>
+__global__ void __launch_bounds__(256)
+    k_cnns_t(const float4* __restrict__ sp, const float4* __restrict__ nlo, const float4* __restrict__ nhi,
+             const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L, const uint32_t* __restrict__ list,
+             const uint32_t* __restrict__ n_list, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
+             uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
+             uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
+             uint32_t* __restrict__ defer, uint32_t* __restrict__ n_defer, unsigned long long* __restrict__ stats)
+{
+    constexpr int kTStack = 48;
+    const uint32_t total = *n_list;
+    for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
+        const uint32_t qi = base0 + threadIdx.x;
+        const bool listed = qi < total;
+        const uint32_t me = listed ? list[qi] : 0u;
+        const uint32_t labp = listed ? lab[me] : kEmpty;
+        const float lb0 = listed ? lbp[me] : 0.f;
+        bool valid = listed, deferred = false;
+        float cb = INFINITY;
+        if (listed) {
+            const uint64_t k = __ldcg(&ckey[labp]);
+            cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+            if (lb0 > cb) {
+                valid = false;  // cannot hold its component's minimum this round
+            } else if (pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
+                valid = false;  // not among its component's most promising points: second pass
+                deferred = true;
+            }
+        }
+        warp_append(deferred, me, defer, n_defer);
+
+        bool record = false;
+        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
+        if (valid) {
+            const float4 P = sp[me];
+            const int op = __float_as_int(P.w);
+            float bd = INFINITY, cut = INFINITY;
+            int bo = INT_MAX, bs = -1;
+
+            auto scan_leaf = [&](uint32_t leaf) {
+                const uint32_t b = leaf * 32;
+                const uint32_t m = min(32u, n - b);
+                ++st_leaves;
+                st_cands += m;
+                for (uint32_t j = 0; j < m; ++j) {
+                    const uint32_t q = b + j;
+                    if (__ldg(&lab[q]) == labp) continue;
+                    const float4 c = __ldg(&sp[q]);
+                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                    const int oq = __float_as_int(c.w);
+                    if (d2 < bd || (d2 == bd && oq < bo)) {
+                        bd = d2;
+                        bo = oq;
+                        bs = (int)q;
+                    }
+                }
+            };
+            // lower bound of d2 over a node's box, or +inf when the node cannot help
+            auto node_lb = [&](uint32_t node) -> float {
+                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                if (lo.x > hi.x) return INFINITY;
+                if (__ldg(&nlab[node]) == labp) return INFINITY;  // all in the query's component
+                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+                return d2_of<D>(gx, gy, gz);
+            };
+
+            const uint32_t own = me >> 5;
+            if (__ldg(&nlab[L + own]) != labp) scan_leaf(own);
+            uint32_t stack[kTStack];
+            int top = 0;
+            stack[top++] = 1u;
+            while (top > 0) {
+                const uint32_t node = stack[--top];
+                ++st_nodes;
+                if (node >= L) {
+                    if (node - L == own) continue;
+                    // bound re-checked: bd may have shrunk since the push
+                    const float lb = node_lb(node);
+                    if (lb > bd) continue;
+                    if (lb > cb) {
+                        cut = fminf(cut, lb);
+                        continue;
+                    }
+                    scan_leaf(node - L);
+                    const uint64_t k = __ldcg(&ckey[labp]);
+                    cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+                    continue;
+                }
+                const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                const float l0 = node_lb(c0), l1 = node_lb(c1);
+                const float lim = fminf(bd, cb);
+                // push the farther child first so the nearer one is searched next
+                const bool near0 = l0 <= l1;
+                const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
+                const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
+                if (top + 2 > kTStack) break;  // cannot happen for trees of depth < 46
+                if (lf <= lim) stack[top++] = cf;
+                else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
+                if (ln <= lim) stack[top++] = cn;
+                else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
+            }
+            const bool exact = bs >= 0 && bd < cut;
+            lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
+            if (bs >= 0) {
+                const uint32_t mn = (uint32_t)min(op, bo);
+                const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
+                selq[me] = exact ? (uint32_t)bs : kNone;
+                selkey[me] = key;
+                if (key <= __ldcg(&ckey[labp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                selq[me] = kNone;
+            }
+        }
+        warp_append(record, me, prov, n_prov);
+        if (stats) {
+            unsigned long long a = st_leaves, b = st_nodes, c = st_cands, q = valid ? 1ull : 0ull;
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(kFull, a, o);
+                b += __shfl_xor_sync(kFull, b, o);
+                c += __shfl_xor_sync(kFull, c, o);
+                q += __shfl_xor_sync(kFull, q, o);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&stats[0], a);
+                atomicAdd(&stats[1], b);
+                atomicAdd(&stats[2], c);
+                atomicAdd(&stats[3], 1ull);
+                atomicAdd(&stats[4], q);
+            }
+        }
+    }
+}
+
+__global__ void k_fill_u32(uint32_t* __restrict__ p, uint32_t n, uint32_t v)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+unsigned list_grid(uint64_t upper)
+{
+    uint64_t b = (upper + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 152ull * 16) b = 152ull * 16;
+    return (unsigned)b;
+}
+
+}  // namespace
+
+// Per-round node labels: the component shared by all points of a subtree.
+cudaError_t cnns_node_labels(Ctx& c)
+{
+    cudaError_t e;
+    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
+    const uint32_t L = (uint32_t)c.L;
+    const uint32_t span = L < (uint32_t)kLeavesPerBlock ? L : (uint32_t)kLeavesPerBlock;
+    k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(c.lab.p, (uint32_t)c.n, (uint32_t)c.nchunk, L, span,
+                                                       c.nlab.p);
+    c.launches++;
+    if (L / span >= 2) {
+        k_node_labels_top<<<1, 1024, 0, c.stream>>>(L / span, c.nlab.p);
+        c.launches++;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t cnns_init(Ctx& c)
+{
+    cudaError_t e;
+    const size_t n = (size_t)c.n;
+    if ((e = ensure(c.dirty, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.dirty2, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.lbp, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.clb, n)) != cudaSuccess) return e;
+    k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
+    k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
+    cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
+    c.launches += 2;
+    return cudaGetLastError();
+}
+
+// Reuse pass + two search passes over the dirty points; fills ckey and the
+// provisional winner list exactly like the static-table selection does.
+cudaError_t cnns_select(Ctx& c)
+{
+    DevCounters* d = c.ctr.p;
+    cudaMemsetAsync(&d->n_dirty, 0, 2 * sizeof(uint32_t), c.stream);  // n_dirty, n_dirty2
+    cudaMemsetAsync(&d->n_prov, 0, sizeof(uint32_t), c.stream);
+    k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
+                                                  c.clb.p, c.dirty.p, &d->n_dirty, c.prov.p, &d->n_prov);
+    constexpr int WPB = 4;
+    const unsigned blocks = (unsigned)std::min<int64_t>((c.n + 32 * WPB - 1) / (32 * WPB), 152 * 32);
+    unsigned long long* st = c.profile ? c.nstats.p : nullptr;
+    for (int pass = 1; pass <= 2; ++pass) {
+        const uint32_t* list = pass == 1 ? c.dirty.p : c.dirty2.p;
+        const uint32_t* cnt = pass == 1 ? &d->n_dirty : &d->n_dirty2;
+        if (c.cnns_warp) {
+            if (c.dim == 2)
+                k_cnns<2, WPB><<<blocks, WPB * 32, 0, c.stream>>>(
+                    c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p,
+                    c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2,
+                    st);
+            else
+                k_cnns<3, WPB><<<blocks, WPB * 32, 0, c.stream>>>(
+                    c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p,
+                    c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2,
+                    st);
+        } else {
+            const unsigned tb = list_grid(c.n);
+            if (c.dim == 2)
+                k_cnns_t<2><<<tb, 256, 0, c.stream>>>(c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
+                                                       (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
+                                                       c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
+                                                       c.dirty2.p, &d->n_dirty2, st);
+            else
+                k_cnns_t<3><<<tb, 256, 0, c.stream>>>(c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
+                                                       (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
+                                                       c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
+                                                       c.dirty2.p, &d->n_dirty2, st);
+        }
+        c.nns_launches++;
+    }
+    c.launches += 3;
+    return cudaGetLastError();
+}
+
+}  // namespace emst

@@ -143,7 +143,9 @@ emst_status do_octants(emst_ctx* x)
     if (x->stage != 1) return set_err(x, EMST_ESTATE, "compute_octants: call flatten first");
     c.round++;
     Timed t(x, PH_OCTANTS);
-    if (c.round == 1)
+    if (c.search_mode == 0)
+        EMST_CUDA(x, emst::cnns_node_labels(c), "compute_octants (node labels)");
+    else if (c.round == 1)
         EMST_CUDA(x, emst::nns_full(c), "compute_octants");
     else
         EMST_CUDA(x, emst::nns_recompute_zero(c), "compute_octants (zero recompute)");
@@ -155,7 +157,10 @@ emst_status do_select(emst_ctx* x)
 {
     if (x->stage != 2) return set_err(x, EMST_ESTATE, "find_next_closest: call compute_octants first");
     Timed t(x, PH_SELECT);
-    EMST_CUDA(x, emst::boruvka_select(x->c), "find_next_closest");
+    if (x->c.search_mode == 0)
+        EMST_CUDA(x, emst::cnns_select(x->c), "find_next_closest");
+    else
+        EMST_CUDA(x, emst::boruvka_select(x->c), "find_next_closest");
     x->stage = 3;
     return EMST_OK;
 }
@@ -236,14 +241,15 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     c.launches = 0;
     c.nns_launches = 0;
     if (c.profile) {
-        EMST_CUDA(x, emst::ensure(c.nstats, 4), "alloc");
-        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 4 * sizeof(unsigned long long), c.stream), "stats");
+        EMST_CUDA(x, emst::ensure(c.nstats, 5), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 5 * sizeof(unsigned long long), c.stream), "stats");
     }
     for (double& v : x->ms) v = 0.0;
     {
         Timed t(x, PH_GRID);
         EMST_CUDA(x, emst::grid_build(c), "grid build");
         EMST_CUDA(x, emst::boruvka_init(c), "init");
+        if (c.search_mode == 0) EMST_CUDA(x, emst::cnns_init(c), "init");
     }
     c.round = 0;
     c.finished = false;
@@ -283,6 +289,8 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->warps_per_block > 0) c.warps_per_block = cfg->warps_per_block;
         c.keep_table = cfg->keep_region_table != 0;
         c.profile = cfg->profile != 0;
+        c.search_mode = (cfg->search_mode == 1 || c.keep_table) ? 1 : 0;
+        c.cnns_warp = cfg->search_mode == 2;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking);
@@ -320,6 +328,11 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.nhi);
     emst::release(c.nid);
     emst::release(c.nstats);
+    emst::release(c.nlab);
+    emst::release(c.dirty);
+    emst::release(c.dirty2);
+    emst::release(c.lbp);
+    emst::release(c.clb);
     emst::release(c.cand);
     emst::release(c.cnt);
     emst::release(c.cur);
@@ -520,12 +533,13 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     out->octant_launches = x->c.nns_launches;
     out->rounds = x->c.round;
     if (x->c.profile && x->c.nstats.p) {
-        unsigned long long st[4];
+        unsigned long long st[5];
         EMST_CUDA(x, cudaMemcpy(st, x->c.nstats.p, sizeof(st), cudaMemcpyDeviceToHost), "stats");
         out->leaf_visits = (int64_t)st[0];
         out->node_tests = (int64_t)st[1];
         out->candidates = (int64_t)st[2];
         out->search_warps = (int64_t)st[3];
+        out->search_queries = (int64_t)st[4];
     }
     return EMST_OK;
 }

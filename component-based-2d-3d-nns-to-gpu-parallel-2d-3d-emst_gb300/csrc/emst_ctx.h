@@ -43,7 +43,9 @@ struct DevCounters {
     uint32_t pos0;  // leaf position of input point 0
     uint32_t s_act;
     uint32_t s_roots;
-    uint32_t pad[6];
+    uint32_t n_dirty;
+    uint32_t n_dirty2;
+    uint32_t pad[4];
 };
 
 struct NormParams {
@@ -109,6 +111,12 @@ struct Ctx {
     int64_t launches = 0;
     int64_t nns_launches = 0;
     bool profile = false;
+    int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu)
+    bool cnns_warp = false;   // component search: warp per 32 queries instead of thread per query
+    DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
+    DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
+    DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
+    DevBuf<uint32_t> clb;            // per root: min lbp over its dirty points (float bits)
     DevBuf<unsigned long long> nstats;  // region search: leaf visits, node tests, candidates, warps
 
     int round = 0;        // rounds started
@@ -134,6 +142,10 @@ cudaError_t boruvka_count_other(Ctx& c);
 cudaError_t evaluate_length(Ctx& c, double* d_out);
 cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out);
 cudaError_t table_to_host_order(Ctx& c);
+// cnns.cu
+cudaError_t cnns_init(Ctx& c);
+cudaError_t cnns_node_labels(Ctx& c);
+cudaError_t cnns_select(Ctx& c);
 
 template <typename T>
 cudaError_t ensure(DevBuf<T>& b, size_t n)

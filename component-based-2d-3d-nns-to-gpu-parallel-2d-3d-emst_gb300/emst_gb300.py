@@ -31,7 +31,8 @@ class EmstError(RuntimeError):
 
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_rounds", ctypes.c_int), ("warps_per_block", ctypes.c_int),
-                ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("search_mode", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class Profile(ctypes.Structure):
@@ -39,7 +40,7 @@ class Profile(ctypes.Structure):
                 ("ms_resolve", ctypes.c_double), ("ms_hook", ctypes.c_double), ("ms_flatten", ctypes.c_double),
                 ("launches", ctypes.c_int64), ("octant_launches", ctypes.c_int64), ("rounds", ctypes.c_int64),
                 ("leaf_visits", ctypes.c_int64), ("node_tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
-                ("search_warps", ctypes.c_int64), ("reserved", ctypes.c_int64 * 1)]
+                ("search_warps", ctypes.c_int64), ("search_queries", ctypes.c_int64)]
 
 
 def build(jobs=4):
@@ -92,8 +93,10 @@ def _p(a):
 class Emst:
     """One context = one CUDA stream on one device."""
 
-    def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False):
-        cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0)
+    def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False,
+                 search_mode=0):
+        cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0,
+                     int(search_mode))
         h = ctypes.c_void_p()
         st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:

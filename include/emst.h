@@ -49,7 +49,11 @@ typedef struct {
     int keep_region_table; /* != 0: keep the round-1 region table for
                               emst_get_region_table (n * K * 8 bytes) */
     int profile;           /* != 0: time every phase with CUDA events */
-    int reserved[7];
+    int search_mode;       /* 0: component nearest-neighbour search (default);
+                              1: static-pruning region table, the reference's
+                              computeOctants (implied by keep_region_table);
+                              2: component search, one warp per 32 queries */
+    int reserved[6];
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel
@@ -72,7 +76,7 @@ typedef struct {
     int64_t node_tests;
     int64_t candidates;
     int64_t search_warps;
-    int64_t reserved[1];
+    int64_t search_queries; /* component mode: point searches run (all rounds) */
 } emst_profile;
 
 /* Context lifetime.  Replaces CalculateurEMST::initialize / the static

@@ -42,9 +42,14 @@ def _is_spanning_tree(n, edges):
     return True
 
 
-def test_golden_3000_edges_labels_length(gpu_lib, fixtures):
+MODES = [0, 1, 2]  # 0: component search (default), 1: static region table (reference's computeOctants),
+#                    2: component search, warp per 32 queries
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_golden_3000_edges_labels_length(gpu_lib, fixtures, mode):
     pts = fixtures["pts2d_3000"]
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         e.run()
         uv = e.edges()
@@ -59,12 +64,13 @@ def test_golden_3000_edges_labels_length(gpu_lib, fixtures):
     assert length == pytest.approx(O.length(pts, uv.astype(np.int64)), rel=1e-9)
 
 
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("key,dim", TRACED)
-def test_golden_round_traces(gpu_lib, fixtures, traces, key, dim):
+def test_golden_round_traces(gpu_lib, fixtures, traces, key, dim, mode):
     pts = fixtures[key]
     n = len(pts)
     trace = traces["%dd" % dim]["%drandomCity.%dd" % (n, dim)][0]
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         e.run()
         uv, rounds = e.edges(with_rounds=True)
@@ -112,9 +118,10 @@ def test_region_table_bit_exact(gpu_lib, kind, dim):
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [2, 3, 17, 33, 1000, 6000])
-def test_edge_set_and_rounds_vs_oracle(gpu_lib, kind, dim, n):
+@pytest.mark.parametrize("mode", MODES)
+def test_edge_set_and_rounds_vs_oracle(gpu_lib, kind, dim, n, mode):
     pts = family(kind, n, dim, 1000 + n)
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         e.run()
         uv, rounds = e.edges(with_rounds=True)
@@ -127,13 +134,14 @@ def test_edge_set_and_rounds_vs_oracle(gpu_lib, kind, dim, n):
         assert np.array_equal(_canon(uv), _canon(O.prim(sp)))
 
 
-def test_operator_sequence_equals_run(gpu_lib):
+@pytest.mark.parametrize("mode", MODES)
+def test_operator_sequence_equals_run(gpu_lib, mode):
     pts = family("cluster", 20000, 3, 5)
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         e.run()
         ref_edges = _canon(e.edges())
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         others = []
         for _ in range(100):
@@ -167,9 +175,10 @@ def test_single_point_and_pairs(gpu_lib):
         assert _canon(uv).tolist() == [[0, 1]] and length == pytest.approx(3.0)
 
 
-def test_all_identical_points(gpu_lib):
+@pytest.mark.parametrize("mode", MODES)
+def test_all_identical_points(gpu_lib, mode):
     pts = np.full((777, 3), 0.25, np.float32)
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         e.initialize(pts)
         e.run()
         uv = e.edges()
@@ -213,12 +222,14 @@ def test_device_entry_point_matches_host(gpu_lib):
     assert d_len.item() == pytest.approx(len_h, rel=1e-12)
 
 
-def test_repeat_runs_are_identical(gpu_lib):
-    """Union-find compression runs concurrently; repeated solves in one
-    context (buffers holding the previous solve's data) must agree exactly."""
+@pytest.mark.parametrize("mode", MODES)
+def test_repeat_runs_are_identical(gpu_lib, mode):
+    """Union-find compression and the searches run concurrently; repeated
+    solves in one context (buffers holding the previous solve's data) must
+    agree exactly."""
     pts = family("cluster", 6000, 3, 7000)
     ref = None
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(search_mode=mode) as e:
         for _ in range(200):
             uv, length = e.solve(pts)
             if ref is None:
@@ -255,3 +266,15 @@ def test_full_size_structure(gpu_lib, name, n):
     assert np.array_equal(d2[rows].view(np.uint32), td.view(np.uint32))
     mst = O.kruskal_table(ids, d2)
     assert np.array_equal(_canon(mst), _canon(uv))
+    # the component search reaches the same tree, round by round
+    with gpu_lib.Emst(search_mode=1) as e:
+        e.initialize(pts)
+        e.run()
+        uv1, r1 = e.edges(with_rounds=True)
+    with gpu_lib.Emst(search_mode=0) as e:
+        e.initialize(pts)
+        e.run()
+        uv0, r0 = e.edges(with_rounds=True)
+    assert np.array_equal(_canon(uv0), _canon(uv))
+    for k in range(1, int(r1.max()) + 1):
+        assert np.array_equal(_canon(uv0[r0 == k]), _canon(uv1[r1 == k]))
