@@ -320,9 +320,10 @@ __global__ void __launch_bounds__(WPB * 32)
 // last, so every query sees good bounds early (queries of later rounds are
 // sparse, and one warp-wide order would serve only some of them).
 template <int D>
-__global__ void __launch_bounds__(256)
-    k_cnns_t(const float4* __restrict__ sp, const float4* __restrict__ nlo, const float4* __restrict__ nhi,
-             const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L, const uint32_t* __restrict__ list,
+__global__ void __launch_bounds__(256, 4)
+    k_cnns_t(const float4* __restrict__ spl, const uint32_t* __restrict__ perm, const float4* __restrict__ nlo,
+             const float4* __restrict__ nhi, const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L,
+             const uint32_t* __restrict__ list,
              const uint32_t* __restrict__ n_list, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
              uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
              uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
@@ -353,26 +354,42 @@ __global__ void __launch_bounds__(256)
         bool record = false;
         uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
         if (valid) {
-            const float4 P = sp[me];
-            const int op = __float_as_int(P.w);
+            const float4 P = spl[me];
+            const int op = (int)perm[me];
             float bd = INFINITY, cut = INFINITY;
-            int bo = INT_MAX, bs = -1;
+            int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
+            int bs = -1;  // leaf position of the best
 
+            // spl holds (x, y, z, label bits); input ids are needed only to
+            // break exact d2 ties and for the final key.
             auto scan_leaf = [&](uint32_t leaf) {
                 const uint32_t b = leaf * 32;
                 const uint32_t m = min(32u, n - b);
                 ++st_leaves;
                 st_cands += m;
-                for (uint32_t j = 0; j < m; ++j) {
-                    const uint32_t q = b + j;
-                    if (__ldg(&lab[q]) == labp) continue;
-                    const float4 c = __ldg(&sp[q]);
-                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                    const int oq = __float_as_int(c.w);
-                    if (d2 < bd || (d2 == bd && oq < bo)) {
-                        bd = d2;
-                        bo = oq;
-                        bs = (int)q;
+                const float own = __uint_as_float(labp);
+                for (uint32_t j = 0; j < m; j += 4) {
+                    float4 c[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, own);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (__float_as_uint(c[k].w) == labp) continue;
+                        const float d2 =
+                            d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z));
+                        if (d2 < bd) {
+                            bd = d2;
+                            bs = (int)(b + j + k);
+                            bo = -1;
+                        } else if (d2 == bd) {
+                            const int oq = (int)__ldg(&perm[b + j + k]);
+                            if (bo < 0) bo = (int)__ldg(&perm[bs]);
+                            if (oq < bo) {
+                                bo = oq;
+                                bs = (int)(b + j + k);
+                            }
+                        }
                     }
                 }
             };
@@ -425,6 +442,7 @@ __global__ void __launch_bounds__(256)
             const bool exact = bs >= 0 && bd < cut;
             lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
             if (bs >= 0) {
+                if (bo < 0) bo = (int)__ldg(&perm[bs]);
                 const uint32_t mn = (uint32_t)min(op, bo);
                 const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
                 selq[me] = exact ? (uint32_t)bs : kNone;
@@ -457,6 +475,17 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Per round: points in leaf order with their current component label.
+__global__ void k_pack_spl(uint32_t n, const float4* __restrict__ sp, const uint32_t* __restrict__ lab,
+                           float4* __restrict__ spl)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 v = sp[i];
+    v.w = __uint_as_float(lab[i]);
+    spl[i] = v;
+}
+
 __global__ void k_fill_u32(uint32_t* __restrict__ p, uint32_t n, uint32_t v)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -483,6 +512,11 @@ cudaError_t cnns_node_labels(Ctx& c)
     k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(c.lab.p, (uint32_t)c.n, (uint32_t)c.nchunk, L, span,
                                                        c.nlab.p);
     c.launches++;
+    if (!c.cnns_warp) {
+        if ((e = ensure(c.spl, (size_t)c.n)) != cudaSuccess) return e;
+        k_pack_spl<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.sp.p, c.lab.p, c.spl.p);
+        c.launches++;
+    }
     if (L / span >= 2) {
         k_node_labels_top<<<1, 1024, 0, c.stream>>>(L / span, c.nlab.p);
         c.launches++;
@@ -534,12 +568,12 @@ cudaError_t cnns_select(Ctx& c)
         } else {
             const unsigned tb = list_grid(c.n);
             if (c.dim == 2)
-                k_cnns_t<2><<<tb, 256, 0, c.stream>>>(c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
+                k_cnns_t<2><<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
                                                        (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
                                                        c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
                                                        c.dirty2.p, &d->n_dirty2, st);
             else
-                k_cnns_t<3><<<tb, 256, 0, c.stream>>>(c.sp.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
+                k_cnns_t<3><<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
                                                        (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
                                                        c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
                                                        c.dirty2.p, &d->n_dirty2, st);

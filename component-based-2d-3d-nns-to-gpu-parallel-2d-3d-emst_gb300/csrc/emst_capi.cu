@@ -333,6 +333,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.dirty2);
     emst::release(c.lbp);
     emst::release(c.clb);
+    emst::release(c.spl);
     emst::release(c.cand);
     emst::release(c.cnt);
     emst::release(c.cur);

@@ -116,6 +116,7 @@ struct Ctx {
     DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
     DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
+    DevBuf<float4> spl;              // per round: (x, y, z, component label) in leaf order
     DevBuf<uint32_t> clb;            // per root: min lbp over its dirty points (float bits)
     DevBuf<unsigned long long> nstats;  // region search: leaf visits, node tests, candidates, warps
 
