@@ -109,13 +109,14 @@ query point (float4) and its label, write partner + key, one 8-byte atomicMin.""
 PHASES = ["ms_grid", "ms_octants", "ms_select", "ms_resolve", "ms_hook", "ms_flatten"]
 
 
-def traffic_from_profile(name, n):
-    """dram bytes per point of k_nns from the committed ncu summary, scaled to n."""
-    path = os.path.join(ROOT, "profiles", "k_nns_%s.md" % name)
+def traffic_from_profile(name):
+    """Mean DRAM bytes (read + write) per launch of the dominant kernel, from the
+    committed ncu summary profiles/<kernel>_<workload>.md (null if absent)."""
+    path = os.path.join(ROOT, "profiles", "%s.md" % name)
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_point:"):
-                return float(line.split(":")[1]) * n
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
     except OSError:
         pass
     return None
@@ -203,8 +204,13 @@ def main():
     d_len = torch.empty(1, dtype=torch.float64, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
-    ctx = E.Emst(device=local, profile=True, search_mode=args.mode)
+    # timed context: the default path (the component search runs its round loop
+    # as one CUDA graph); a separate profiled context (host-driven rounds with
+    # per-phase CUDA events) gives the phase split and the kernel times
+    ctx = E.Emst(device=local, search_mode=args.mode)
     ctx.set_stream(stream.cuda_stream)
+    pctx = E.Emst(device=local, profile=True, search_mode=args.mode)
+    pctx.set_stream(stream.cuda_stream)
 
     def step():
         return ctx.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
@@ -234,10 +240,6 @@ def main():
         ev1.synchronize()
         dev_ms.append(ev0.elapsed_time(ev1))
         prof = ctx.profile()
-        for k in PHASES:
-            phase[k] += prof[k]
-        for k in stat:
-            stat[k] += prof[k]
         launches += prof["launches"]
         rounds = prof["rounds"]
         assert ne == n - 1
@@ -250,6 +252,18 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = world * n * args.steps / (total_ms / 1e3) / 1e6
+
+    # profiled run(s): phase split, search counters and the dominant kernel's time
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        pctx.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+        prof = pctx.profile()
+        for k in PHASES:
+            phase[k] += prof[k]
+        for k in stat:
+            stat[k] += prof[k]
+    pctx.close()
 
     # e2e through the public host API: pinned points in, host edges + length out
     host_pts = torch.from_numpy(pts).pin_memory().numpy()
@@ -278,7 +292,7 @@ def main():
         per_launch_ms = phase["ms_octants"] / n_launch
         alg = nns_bytes(n, dim) * K / n_launch
     achieved = alg / (per_launch_ms / 1e3) / 1e9
-    traffic = traffic_from_profile("%s_%s" % (kernel, args.workload), n)
+    traffic = traffic_from_profile("%s_%s" % (kernel, args.workload)) if args.n is None else None
     search = {"leaf_visits_per_warp": stat["leaf_visits"] / max(stat["search_warps"], 1),
               "node_tests_per_warp": stat["node_tests"] / max(stat["search_warps"], 1),
               "candidates_per_point": stat["candidates"] / (n * K),

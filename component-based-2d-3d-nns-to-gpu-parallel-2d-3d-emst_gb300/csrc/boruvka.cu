@@ -46,6 +46,7 @@ __global__ void k_init(uint32_t n, uint32_t* __restrict__ lab, uint32_t* __restr
                        uint32_t* __restrict__ roots, uint32_t* __restrict__ act, uint64_t* __restrict__ ckey,
                        uint64_t* __restrict__ cmax)
 {
+    // roots: first half holds the current roots (DevCounters::rpar = 0)
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     lab[i] = i;
@@ -118,14 +119,16 @@ __global__ void k_resolve(const uint32_t* __restrict__ prov, const uint32_t* __r
     }
 }
 
-__global__ void k_hook(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+__global__ void k_hook(const uint32_t* __restrict__ roots2, const DevCounters* dc,
                        const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
                        const uint64_t* __restrict__ ckey, const uint64_t* __restrict__ cmax,
                        const uint32_t* __restrict__ selq, uint32_t* __restrict__ par, int32_t* __restrict__ edges,
-                       int32_t* __restrict__ eround, uint32_t* __restrict__ n_edges, int round, uint32_t n,
+                       int32_t* __restrict__ eround, uint32_t* __restrict__ n_edges, uint32_t n,
                        uint32_t* __restrict__ err)
 {
-    const uint32_t total = *n_roots;
+    const uint32_t total = dc->n_roots;
+    const int round = dc->round;
+    const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool emit = false;
@@ -169,10 +172,11 @@ __global__ void k_hook(const uint32_t* __restrict__ roots, const uint32_t* __res
 // Path-halving walk from every previous root to its new root.  The hook
 // graph is acyclic, so a walk ends within n_roots steps; the step cap only
 // turns an internal error into an error flag instead of an endless loop.
-__global__ void k_jump(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+__global__ void k_jump(const uint32_t* __restrict__ roots2, const DevCounters* __restrict__ dc, uint32_t n,
                        uint32_t* __restrict__ par, uint32_t* __restrict__ err)
 {
-    const uint32_t total = *n_roots;
+    const uint32_t total = dc->n_roots;
+    const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const uint32_t c = roots[i];
         uint32_t x = c;
@@ -212,12 +216,16 @@ __global__ void k_relabel(uint32_t n, uint32_t* __restrict__ lab, const uint32_t
     }
 }
 
-__global__ void k_compact_roots(const uint32_t* __restrict__ roots, const uint32_t* __restrict__ n_roots,
+// Surviving roots of the current half go to the other half; the count
+// of the current list was moved to s_roots by k_flatten_begin.
+__global__ void k_compact_roots(uint32_t* __restrict__ roots2, DevCounters* dc, uint32_t n,
                                 const uint32_t* __restrict__ par, uint64_t* __restrict__ ckey,
-                                uint64_t* __restrict__ cmax, uint32_t* __restrict__ clb,
-                                uint32_t* __restrict__ roots_next, uint32_t* __restrict__ n_roots_next)
+                                uint64_t* __restrict__ cmax, uint32_t* __restrict__ clb)
 {
-    const uint32_t total = *n_roots;
+    const uint32_t total = dc->s_roots;
+    const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
+    uint32_t* roots_next = roots2 + (size_t)(dc->rpar ^ 1u) * n;
+    uint32_t* n_roots_next = &dc->n_roots;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool keep = false;
@@ -295,6 +303,36 @@ unsigned list_grid(uint64_t upper)
 
 }  // namespace
 
+__global__ void k_flatten_begin(DevCounters* dc)
+{
+    dc->s_roots = dc->n_roots;
+    dc->n_roots = 0;
+}
+
+__global__ void k_flatten_end(DevCounters* dc) { dc->rpar ^= 1u; }
+
+// Start of a round: per-round counters to zero, round number + 1.
+__global__ void k_round_tick(DevCounters* dc)
+{
+    dc->round += 1;
+    dc->n_dirty = 0;
+    dc->n_dirty2 = 0;
+    dc->n_prov = 0;
+}
+
+// End of a round (after the flatten): record the cumulative edge count and
+// decide, on the device, whether another round runs.  The round cap bounds
+// the loop whatever the data.
+__global__ void k_round_end(DevCounters* dc, int64_t* cum, int max_rounds, cudaGraphConditionalHandle h)
+{
+    const int r = dc->round;
+    if (r >= 1 && r <= 128) cum[r - 1] = dc->n_edges;
+    const bool progress = dc->n_edges != dc->prev_edges;
+    dc->prev_edges = dc->n_edges;
+    const bool more = dc->err == 0 && dc->n_roots > 1 && progress && r < max_rounds;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
 cudaError_t boruvka_init(Ctx& c)
 {
     cudaError_t e;
@@ -307,8 +345,8 @@ cudaError_t boruvka_init(Ctx& c)
     if ((e = ensure(c.cmax, n)) != cudaSuccess) return e;
     if ((e = ensure(c.act, n)) != cudaSuccess) return e;
     if ((e = ensure(c.act2, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.roots, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.roots2, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.roots, 2 * n)) != cudaSuccess) return e;
+    if ((e = ensure(c.dcum, 128)) != cudaSuccess) return e;
     if ((e = ensure(c.prov, n)) != cudaSuccess) return e;
     if ((e = ensure(c.edges, 2 * (n > 1 ? n - 1 : 1))) != cudaSuccess) return e;
     if ((e = ensure(c.eround, n > 1 ? n - 1 : 1)) != cudaSuccess) return e;
@@ -323,15 +361,28 @@ cudaError_t boruvka_init(Ctx& c)
 cudaError_t boruvka_flatten(Ctx& c)
 {
     DevCounters* d = c.ctr.p;
-    k_jump<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->n_roots, c.par.p, &d->err);
-    k_relabel<<<blocks_for((c.n + 3) / 4, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.par.p);
-    cudaMemcpyAsync(&d->s_roots, &d->n_roots, sizeof(uint32_t), cudaMemcpyDeviceToDevice, c.stream);
-    cudaMemsetAsync(&d->n_roots, 0, sizeof(uint32_t), c.stream);
-    k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->s_roots, c.par.p, c.ckey.p, c.cmax.p,
-                                                                c.search_mode == 0 ? c.clb.p : nullptr, c.roots2.p,
-                                                                &d->n_roots);
-    std::swap(c.roots.p, c.roots2.p);
-    c.launches += 3;
+    const uint32_t n = (uint32_t)c.n;
+    k_jump<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, n, c.par.p, &d->err);
+    k_relabel<<<blocks_for((c.n + 3) / 4, 256), 256, 0, c.stream>>>(n, c.lab.p, c.par.p);
+    k_flatten_begin<<<1, 1, 0, c.stream>>>(d);
+    k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, n, c.par.p, c.ckey.p, c.cmax.p,
+                                                                c.search_mode == 0 ? c.clb.p : nullptr);
+    k_flatten_end<<<1, 1, 0, c.stream>>>(d);
+    c.launches += 5;
+    return cudaGetLastError();
+}
+
+cudaError_t round_tick(Ctx& c)
+{
+    k_round_tick<<<1, 1, 0, c.stream>>>(c.ctr.p);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+cudaError_t round_end(Ctx& c, cudaGraphConditionalHandle h)
+{
+    k_round_end<<<1, 1, 0, c.stream>>>(c.ctr.p, c.dcum.p, c.max_rounds, h);
+    c.launches++;
     return cudaGetLastError();
 }
 
@@ -367,9 +418,9 @@ cudaError_t boruvka_resolve(Ctx& c)
 cudaError_t boruvka_hook(Ctx& c)
 {
     DevCounters* d = c.ctr.p;
-    k_hook<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, &d->n_roots, c.lab.p, c.perm.p, c.ckey.p, c.cmax.p,
-                                                       c.selq.p, c.par.p, c.edges.p, c.eround.p, &d->n_edges,
-                                                       c.round, (uint32_t)c.n, &d->err);
+    k_hook<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, c.lab.p, c.perm.p, c.ckey.p, c.cmax.p, c.selq.p,
+                                                       c.par.p, c.edges.p, c.eround.p, &d->n_edges, (uint32_t)c.n,
+                                                       &d->err);
     c.launches++;
     return cudaGetLastError();
 }

@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(256, 4)
                 deferred = true;
             }
         }
+        __syncwarp();
         warp_append(deferred, me, defer, n_defer);
 
         bool record = false;
@@ -455,6 +456,10 @@ __global__ void __launch_bounds__(256, 4)
                 selq[me] = kNone;
             }
         }
+        // Reconverge the warp before its next 32 queries: without this the
+        // lanes of a diverged warp drift into different iterations and the
+        // next traversals run with a fraction of the warp active.
+        __syncwarp();
         warp_append(record, me, prov, n_prov);
         if (stats) {
             unsigned long long a = st_leaves, b = st_nodes, c = st_cands, q = valid ? 1ull : 0ull;
@@ -506,7 +511,7 @@ unsigned list_grid(uint64_t upper)
 cudaError_t cnns_node_labels(Ctx& c)
 {
     cudaError_t e;
-    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;  // no-op after cnns_init
     const uint32_t L = (uint32_t)c.L;
     const uint32_t span = L < (uint32_t)kLeavesPerBlock ? L : (uint32_t)kLeavesPerBlock;
     k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(c.lab.p, (uint32_t)c.n, (uint32_t)c.nchunk, L, span,
@@ -532,6 +537,8 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.dirty2, n)) != cudaSuccess) return e;
     if ((e = ensure(c.lbp, n)) != cudaSuccess) return e;
     if ((e = ensure(c.clb, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
     cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
@@ -543,9 +550,7 @@ cudaError_t cnns_init(Ctx& c)
 // provisional winner list exactly like the static-table selection does.
 cudaError_t cnns_select(Ctx& c)
 {
-    DevCounters* d = c.ctr.p;
-    cudaMemsetAsync(&d->n_dirty, 0, 2 * sizeof(uint32_t), c.stream);  // n_dirty, n_dirty2
-    cudaMemsetAsync(&d->n_prov, 0, sizeof(uint32_t), c.stream);
+    DevCounters* d = c.ctr.p;  // n_dirty, n_dirty2, n_prov were zeroed by the round tick
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
                                                   c.clb.p, c.dirty.p, &d->n_dirty, c.prov.p, &d->n_prov);
     constexpr int WPB = 4;

@@ -27,6 +27,11 @@ struct emst_ctx {
     std::vector<Pending> pending;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
     double ms[6] = {0, 0, 0, 0, 0, 0};
+    // the whole round loop as one CUDA graph (conditional WHILE node)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<const void*> gkey;
+    int64_t body_launches = 0;
 };
 
 namespace {
@@ -143,6 +148,7 @@ emst_status do_octants(emst_ctx* x)
     if (x->stage != 1) return set_err(x, EMST_ESTATE, "compute_octants: call flatten first");
     c.round++;
     Timed t(x, PH_OCTANTS);
+    EMST_CUDA(x, emst::round_tick(c), "round tick");
     if (c.search_mode == 0)
         EMST_CUDA(x, emst::cnns_node_labels(c), "compute_octants (node labels)");
     else if (c.round == 1)
@@ -262,8 +268,111 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     return EMST_OK;
 }
 
+void drop_graph(emst_ctx* x)
+{
+    if (x->gexec) cudaGraphExecDestroy(x->gexec);
+    if (x->graph) cudaGraphDestroy(x->graph);
+    x->gexec = nullptr;
+    x->graph = nullptr;
+    x->gkey.clear();
+}
+
+// One round of the component search, in stream order (captured once).
+emst_status enqueue_round(emst_ctx* x, cudaGraphConditionalHandle h)
+{
+    Ctx& c = x->c;
+    EMST_CUDA(x, emst::round_tick(c), "round tick");
+    EMST_CUDA(x, emst::cnns_node_labels(c), "node labels");
+    EMST_CUDA(x, emst::cnns_select(c), "find_next_closest");
+    EMST_CUDA(x, emst::boruvka_resolve(c), "find_min_pair");
+    EMST_CUDA(x, emst::boruvka_hook(c), "connect_union");
+    EMST_CUDA(x, emst::boruvka_flatten(c), "flatten");
+    EMST_CUDA(x, emst::round_end(c, h), "round end");
+    return EMST_OK;
+}
+
+// Build (or reuse) the graph: a WHILE node whose body is one round; the
+// round-end kernel sets the condition on the device, so the whole loop runs
+// without a host round trip.  The body is captured on the context's own
+// stream (the caller's stream may be the legacy default stream).
+emst_status build_graph(emst_ctx* x)
+{
+    Ctx& c = x->c;
+    std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
+                                    c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
+                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p};
+    if (x->gexec && key == x->gkey) return EMST_OK;
+    drop_graph(x);
+    cudaGraph_t g = nullptr, body = nullptr;
+    cudaGraphConditionalHandle h;
+    cudaGraphNode_t node;
+    EMST_CUDA(x, cudaGraphCreate(&g, 0), "graph");
+    x->graph = g;
+    EMST_CUDA(x, cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault), "graph handle");
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    EMST_CUDA(x, cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp), "graph node");
+    body = cp.conditional.phGraph_out[0];
+    cudaStream_t work = c.stream;
+    const uint32_t save_roots = c.n_roots, save_act = c.n_act;
+    const int64_t save_launches = c.launches;
+    c.stream = c.own_stream;
+    c.n_roots = (uint32_t)c.n;  // grid sizes: upper bounds (every kernel reads its count on the device)
+    c.n_act = (uint32_t)c.n;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    emst_status st = e == cudaSuccess ? enqueue_round(x, h) : cuda_err(x, e, "begin capture");
+    cudaGraph_t captured = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c.stream, &captured);
+    c.stream = work;
+    c.n_roots = save_roots;
+    c.n_act = save_act;
+    x->body_launches = c.launches - save_launches;
+    c.launches = save_launches;
+    if (st != EMST_OK) return st;
+    EMST_CUDA(x, e2, "end capture");
+    EMST_CUDA(x, cudaGraphInstantiate(&x->gexec, g, 0), "graph instantiate");
+    x->gkey = key;
+    return EMST_OK;
+}
+
+emst_status run_graph(emst_ctx* x)
+{
+    Ctx& c = x->c;
+    emst_status st = read_counters(x);
+    if (st != EMST_OK) return st;
+    if (c.n_roots > 1) {
+        if ((st = build_graph(x)) != EMST_OK) return st;
+        EMST_CUDA(x, cudaGraphLaunch(x->gexec, c.stream), "graph launch");
+        if ((st = read_counters(x)) != EMST_OK) return st;
+        c.round = c.hctr->round;
+        c.launches += (int64_t)c.round * x->body_launches;
+        c.nns_launches += 2 * (int64_t)c.round;
+        int64_t cum[128];
+        const int r = c.round < 128 ? c.round : 128;
+        if (r > 0) {
+            EMST_CUDA(x, cudaMemcpyAsync(cum, c.dcum.p, sizeof(int64_t) * r, cudaMemcpyDeviceToHost, c.stream),
+                      "round stats");
+            EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+        }
+        c.cum_edges.assign(cum, cum + r);
+    }
+    c.finished = true;
+    x->stage = 0;
+    if (c.n_roots > 1) {
+        if (c.round >= c.max_rounds) return set_err(x, EMST_ENOCONVERGE, "round cap reached");
+        return set_err(x, EMST_ENOCONVERGE, "a round added no edge while several components remain");
+    }
+    return EMST_OK;
+}
+
 emst_status do_run(emst_ctx* x)
 {
+    Ctx& c = x->c;
+    if (c.search_mode == 0 && !c.cnns_warp && c.use_graph && !c.profile && c.round == 0 && x->stage == 0)
+        return run_graph(x);
     int more = 1;
     while (more) {
         emst_status st = do_activate(x, &more);
@@ -291,6 +400,7 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         c.profile = cfg->profile != 0;
         c.search_mode = (cfg->search_mode == 1 || c.keep_table) ? 1 : 0;
         c.cnns_warp = cfg->search_mode == 2;
+        c.use_graph = cfg->host_rounds == 0;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking);
@@ -349,7 +459,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.act);
     emst::release(c.act2);
     emst::release(c.roots);
-    emst::release(c.roots2);
+    emst::release(c.dcum);
     emst::release(c.prov);
     emst::release(c.zero);
     emst::release(c.zero2);
@@ -366,6 +476,7 @@ emst_status emst_destroy(emst_ctx* x)
     }
     if (c.hctr) cudaFreeHost(c.hctr);
     if (c.hlen) cudaFreeHost(c.hlen);
+    drop_graph(x);
     if (c.own_stream) cudaStreamDestroy(c.own_stream);
     delete x;
     return EMST_OK;

@@ -45,7 +45,10 @@ struct DevCounters {
     uint32_t s_roots;
     uint32_t n_dirty;
     uint32_t n_dirty2;
-    uint32_t pad[4];
+    uint32_t rpar;        // which half of the 2n roots buffer holds the current roots
+    int32_t round;        // rounds started (device copy, read by k_hook)
+    uint32_t prev_edges;  // edge count at the end of the previous round
+    uint32_t pad;
 };
 
 struct NormParams {
@@ -98,7 +101,8 @@ struct Ctx {
 
     DevBuf<uint32_t> lab, par, selq;
     DevBuf<uint64_t> ckey, cmax, selkey;
-    DevBuf<uint32_t> act, act2, roots, roots2, prov, zero, zero2;
+    DevBuf<uint32_t> act, act2, roots, prov, zero, zero2;  // roots: 2n, halves by DevCounters::rpar
+    DevBuf<int64_t> dcum;                                  // per round: cumulative edges (device)
     uint32_t n_act = 0, n_roots = 0, n_zero = 0;
     DevBuf<int32_t> edges, eround;
     DevBuf<DevCounters> ctr;
@@ -113,6 +117,7 @@ struct Ctx {
     bool profile = false;
     int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu)
     bool cnns_warp = false;   // component search: warp per 32 queries instead of thread per query
+    bool use_graph = true;    // component search: run the round loop as one CUDA graph
     DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
     DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
@@ -140,6 +145,8 @@ cudaError_t boruvka_select(Ctx& c);
 cudaError_t boruvka_resolve(Ctx& c);
 cudaError_t boruvka_hook(Ctx& c);
 cudaError_t boruvka_count_other(Ctx& c);
+cudaError_t round_tick(Ctx& c);
+cudaError_t round_end(Ctx& c, cudaGraphConditionalHandle h);
 cudaError_t evaluate_length(Ctx& c, double* d_out);
 cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out);
 cudaError_t table_to_host_order(Ctx& c);

@@ -32,7 +32,7 @@ class EmstError(RuntimeError):
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_rounds", ctypes.c_int), ("warps_per_block", ctypes.c_int),
                 ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("search_mode", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("host_rounds", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class Profile(ctypes.Structure):
@@ -94,9 +94,9 @@ class Emst:
     """One context = one CUDA stream on one device."""
 
     def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False,
-                 search_mode=0):
+                 search_mode=0, host_rounds=False):
         cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0,
-                     int(search_mode))
+                     int(search_mode), 1 if host_rounds else 0)
         h = ctypes.c_void_p()
         st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:

@@ -53,7 +53,9 @@ typedef struct {
                               1: static-pruning region table, the reference's
                               computeOctants (implied by keep_region_table);
                               2: component search, one warp per 32 queries */
-    int reserved[6];
+    int host_rounds;       /* != 0: drive the component search's rounds from
+                              the host instead of one CUDA graph */
+    int reserved[5];
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel

@@ -159,6 +159,26 @@ def test_operator_sequence_equals_run(gpu_lib, mode):
         assert len(set(e.labels().tolist())) == 1
 
 
+@pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 50000), ("uniform", 2, 30000), ("dups", 3, 5000),
+                                        ("uniform", 2, 2)])
+def test_graph_loop_matches_host_loop(gpu_lib, kind, dim, n):
+    """emst_run in the component mode runs the round loop as one CUDA graph with
+    device-side termination; a profiled context runs it from the host.  Same
+    edges, same rounds, same per-round counts."""
+    pts = family(kind, n, dim, 77)
+    out = []
+    for prof in (False, True):
+        with gpu_lib.Emst(profile=prof) as e:
+            e.initialize(pts)
+            e.run()
+            uv, rounds = e.edges(with_rounds=True)
+            out.append((_canon(uv), e.round_stats(), rounds, e.labels()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert list(out[0][1]) == list(out[1][1])
+    assert np.array_equal(np.sort(out[0][2]), np.sort(out[1][2]))
+    assert np.array_equal(out[0][3], out[1][3])
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
