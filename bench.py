@@ -137,6 +137,31 @@ def cpu_baseline(pts, threads, sample_n, seed=0):
     return len(sub) / dt / 1e6, dt, len(sub)
 
 
+def batch_bench(E, device, reps=3):
+    """512-cloud workload (sizes log-uniform 1e3..1e5, half 2D half 3D, uniform
+    or 8-cluster): clouds/s of one batched solve (emst_solve_batch) vs the plain
+    solver launched once per cloud (emst_solve), host buffers in and out."""
+    import emst_workloads as W
+    clouds = W.batch_clouds()
+    total = sum(len(c) for c in clouds)
+    with E.Emst(device=device) as e:
+        e.solve_batch(clouds)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            uvs, _ = e.solve_batch(clouds)
+        tb = (time.perf_counter() - t0) / reps
+        for c in clouds[:8]:
+            e.solve(c)
+        t0 = time.perf_counter()
+        for c in clouds:
+            e.solve(c)
+        tl = time.perf_counter() - t0
+    return {"clouds": len(clouds), "points": total, "batched_clouds_per_s": len(clouds) / tb,
+            "per_cloud_clouds_per_s": len(clouds) / tl, "speedup": tl / tb,
+            "batched_ms": 1e3 * tb, "per_cloud_ms": 1e3 * tl,
+            "note": "wall clock, host points in / host edges + lengths out, same edge sets"}
+
+
 def run_reference(args, pts, dim):
     """The CPU restatement of the reference's path, all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -176,6 +201,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", type=int, default=0, help="0: component search, 1: static region table")
     ap.add_argument("--no-static", action="store_true", help="skip the one-step static-table comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-cloud batch comparison")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -313,6 +339,10 @@ def main():
             static = {"value": n / (e0.elapsed_time(e1) / 1e3) / 1e6, "unit": "Mpoints/s", "steps": 1,
                       "note": "static-pruning region table (the reference's computeOctants), same edge set"}
 
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = batch_bench(E, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, m = cpu_baseline(pts, 1, args.cpu_sample)
@@ -333,7 +363,7 @@ def main():
                              "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                              "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
                              "peak_kind": peak_kind},
-                "phase_ms": phase_ms, "static_table_mode": static,
+                "phase_ms": phase_ms, "static_table_mode": static, "batch512": batch,
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
                         "d2h_bytes_per_step": int(8 * (n - 1) + 8)},

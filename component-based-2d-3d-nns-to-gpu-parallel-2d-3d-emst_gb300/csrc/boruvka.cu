@@ -329,7 +329,7 @@ __global__ void k_round_end(DevCounters* dc, int64_t* cum, int max_rounds, cudaG
     if (r >= 1 && r <= 128) cum[r - 1] = dc->n_edges;
     const bool progress = dc->n_edges != dc->prev_edges;
     dc->prev_edges = dc->n_edges;
-    const bool more = dc->err == 0 && dc->n_roots > 1 && progress && r < max_rounds;
+    const bool more = dc->err == 0 && dc->n_roots > dc->n_target && progress && r < max_rounds;
     cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 

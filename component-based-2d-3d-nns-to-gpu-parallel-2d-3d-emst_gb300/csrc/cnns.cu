@@ -133,9 +133,11 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, const uint
                     record = old >= key;
                 }
             } else {
-                is_dirty = true;
+                // lbp = +inf: no point outside the component exists (in a batch,
+                // the cloud is one component), and components only grow
                 const uint32_t lb = __float_as_uint(lbp[p]);
-                if (lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
+                is_dirty = lb != 0x7f800000u;
+                if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
             }
         }
         warp_append(is_dirty, p, dirty, n_dirty);
@@ -319,7 +321,9 @@ __global__ void __launch_bounds__(WPB * 32)
 // leaf first, then a depth-first walk from the root pushing the nearer child
 // last, so every query sees good bounds early (queries of later rounds are
 // sparse, and one warp-wide order would serve only some of them).
-template <int D>
+// CL: batched clouds (pcloud / ncloud given); a candidate must share the
+// query's cloud.
+template <int D, bool CL>
 __global__ void __launch_bounds__(256, 4)
     k_cnns_t(const float4* __restrict__ spl, const uint32_t* __restrict__ perm, const float4* __restrict__ nlo,
              const float4* __restrict__ nhi, const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L,
@@ -327,7 +331,8 @@ __global__ void __launch_bounds__(256, 4)
              const uint32_t* __restrict__ n_list, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
              uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
              uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
-             uint32_t* __restrict__ defer, uint32_t* __restrict__ n_defer, unsigned long long* __restrict__ stats)
+             uint32_t* __restrict__ defer, uint32_t* __restrict__ n_defer, const uint32_t* __restrict__ pcloud,
+             const uint32_t* __restrict__ ncloud, unsigned long long* __restrict__ stats)
 {
     constexpr int kTStack = 48;
     const uint32_t total = *n_list;
@@ -357,6 +362,7 @@ __global__ void __launch_bounds__(256, 4)
         if (valid) {
             const float4 P = spl[me];
             const int op = (int)perm[me];
+            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;  // the query's cloud (batches)
             float bd = INFINITY, cut = INFINITY;
             int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
             int bs = -1;  // leaf position of the best
@@ -365,10 +371,17 @@ __global__ void __launch_bounds__(256, 4)
             // break exact d2 ties and for the final key.
             auto scan_leaf = [&](uint32_t leaf) {
                 const uint32_t b = leaf * 32;
+                if (b >= n) return;  // padding leaf (never reached: its bound is +inf)
                 const uint32_t m = min(32u, n - b);
                 ++st_leaves;
                 st_cands += m;
                 const float own = __uint_as_float(labp);
+                // a leaf straddling clouds: check every candidate's cloud
+                bool mixed = false;
+                if (CL) {
+                    const uint32_t r = __ldg(&ncloud[L + leaf]);
+                    mixed = (r >> 16) != (r & 0xffffu);
+                }
                 for (uint32_t j = 0; j < m; j += 4) {
                     float4 c[4];
 #pragma unroll
@@ -377,6 +390,7 @@ __global__ void __launch_bounds__(256, 4)
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         if (__float_as_uint(c[k].w) == labp) continue;
+                        if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
                         const float d2 =
                             d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z));
                         if (d2 < bd) {
@@ -394,11 +408,18 @@ __global__ void __launch_bounds__(256, 4)
                     }
                 }
             };
-            // lower bound of d2 over a node's box, or +inf when the node cannot help
+            // lower bound of d2 over a node's box, or +inf when the node cannot
+            // help (empty, all in the query's component, all in another cloud);
+            // +inf is tested explicitly: best and shared bound may be +inf too
             auto node_lb = [&](uint32_t node) -> float {
                 const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
                 if (lo.x > hi.x) return INFINITY;
                 if (__ldg(&nlab[node]) == labp) return INFINITY;  // all in the query's component
+                if (CL) {
+                    // (first cloud << 16) | last cloud of the node's points
+                    const uint32_t r = __ldg(&ncloud[node]);
+                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;  // all in other clouds
+                }
                 const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
                 const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
                 const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
@@ -417,7 +438,7 @@ __global__ void __launch_bounds__(256, 4)
                     if (node - L == own) continue;
                     // bound re-checked: bd may have shrunk since the push
                     const float lb = node_lb(node);
-                    if (lb > bd) continue;
+                    if (!(lb < INFINITY) || lb > bd) continue;
                     if (lb > cb) {
                         cut = fminf(cut, lb);
                         continue;
@@ -435,9 +456,9 @@ __global__ void __launch_bounds__(256, 4)
                 const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
                 const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
                 if (top + 2 > kTStack) break;  // cannot happen for trees of depth < 46
-                if (lf <= lim) stack[top++] = cf;
+                if (lf < INFINITY && lf <= lim) stack[top++] = cf;
                 else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
-                if (ln <= lim) stack[top++] = cn;
+                if (ln < INFINITY && ln <= lim) stack[top++] = cn;
                 else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
             }
             const bool exact = bs >= 0 && bd < cut;
@@ -507,23 +528,31 @@ unsigned list_grid(uint64_t upper)
 
 }  // namespace
 
-// Per-round node labels: the component shared by all points of a subtree.
+// Tree-node labels: the value (component, or cloud) shared by all points of
+// a subtree, MIXED when they differ.
+cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out)
+{
+    const uint32_t L = (uint32_t)c.L;
+    const uint32_t span = L < (uint32_t)kLeavesPerBlock ? L : (uint32_t)kLeavesPerBlock;
+    k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(labels, (uint32_t)c.n, (uint32_t)c.nchunk, L, span, out);
+    c.launches++;
+    if (L / span >= 2) {
+        k_node_labels_top<<<1, 1024, 0, c.stream>>>(L / span, out);
+        c.launches++;
+    }
+    return cudaGetLastError();
+}
+
+// Per-round node labels (the component shared by all points of a subtree)
+// and the packed (x, y, z, label) points of the thread-per-query search.
 cudaError_t cnns_node_labels(Ctx& c)
 {
     cudaError_t e;
     if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;  // no-op after cnns_init
-    const uint32_t L = (uint32_t)c.L;
-    const uint32_t span = L < (uint32_t)kLeavesPerBlock ? L : (uint32_t)kLeavesPerBlock;
-    k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(c.lab.p, (uint32_t)c.n, (uint32_t)c.nchunk, L, span,
-                                                       c.nlab.p);
-    c.launches++;
+    if ((e = node_labels_of(c, c.lab.p, c.nlab.p)) != cudaSuccess) return e;
     if (!c.cnns_warp) {
         if ((e = ensure(c.spl, (size_t)c.n)) != cudaSuccess) return e;
         k_pack_spl<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.sp.p, c.lab.p, c.spl.p);
-        c.launches++;
-    }
-    if (L / span >= 2) {
-        k_node_labels_top<<<1, 1024, 0, c.stream>>>(L / span, c.nlab.p);
         c.launches++;
     }
     return cudaGetLastError();
@@ -556,6 +585,8 @@ cudaError_t cnns_select(Ctx& c)
     constexpr int WPB = 4;
     const unsigned blocks = (unsigned)std::min<int64_t>((c.n + 32 * WPB - 1) / (32 * WPB), 152 * 32);
     unsigned long long* st = c.profile ? c.nstats.p : nullptr;
+    const uint32_t* pc = c.n_clouds ? c.pcloud.p : nullptr;
+    const uint32_t* nc = c.n_clouds ? c.ncloud.p : nullptr;
     for (int pass = 1; pass <= 2; ++pass) {
         const uint32_t* list = pass == 1 ? c.dirty.p : c.dirty2.p;
         const uint32_t* cnt = pass == 1 ? &d->n_dirty : &d->n_dirty2;
@@ -572,16 +603,11 @@ cudaError_t cnns_select(Ctx& c)
                     st);
         } else {
             const unsigned tb = list_grid(c.n);
-            if (c.dim == 2)
-                k_cnns_t<2><<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
-                                                       (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
-                                                       c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
-                                                       c.dirty2.p, &d->n_dirty2, st);
-            else
-                k_cnns_t<3><<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n,
-                                                       (uint32_t)c.L, list, cnt, c.lab.p, c.ckey.p, c.selq.p,
-                                                       c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass,
-                                                       c.dirty2.p, &d->n_dirty2, st);
+            auto kern = c.dim == 2 ? (pc ? k_cnns_t<2, true> : k_cnns_t<2, false>)
+                                   : (pc ? k_cnns_t<3, true> : k_cnns_t<3, false>);
+            kern<<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L,
+                                           list, cnt, c.lab.p, c.ckey.p, c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,
+                                           c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2, pc, nc, st);
         }
         c.nns_launches++;
     }

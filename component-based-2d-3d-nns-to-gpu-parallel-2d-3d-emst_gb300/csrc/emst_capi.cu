@@ -196,7 +196,7 @@ emst_status do_activate(emst_ctx* x, int* more)
     if (c.finished) return EMST_OK;
     emst_status st = do_flatten(x);
     if (st != EMST_OK) return st;
-    if (c.n_roots <= 1) {
+    if (c.n_roots <= (uint32_t)c.n_nonempty) {
         c.finished = true;
         x->stage = 0;
         return EMST_OK;
@@ -242,6 +242,9 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     std::memset(c.hctr, 0, sizeof(emst::DevCounters));
     c.hctr->n_act = (uint32_t)n;
     c.hctr->n_roots = (uint32_t)n;
+    c.hctr->n_target = 1;
+    c.n_clouds = 0;
+    c.n_nonempty = 1;
     EMST_CUDA(x, cudaMemcpyAsync(c.ctr.p, c.hctr, sizeof(emst::DevCounters), cudaMemcpyHostToDevice, c.stream),
               "counters");
     c.launches = 0;
@@ -300,7 +303,8 @@ emst_status build_graph(emst_ctx* x)
     Ctx& c = x->c;
     std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
                                     c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
-                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p};
+                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p,
+                                    (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
     cudaGraph_t g = nullptr, body = nullptr;
@@ -343,7 +347,7 @@ emst_status run_graph(emst_ctx* x)
     Ctx& c = x->c;
     emst_status st = read_counters(x);
     if (st != EMST_OK) return st;
-    if (c.n_roots > 1) {
+    if (c.n_roots > (uint32_t)c.n_nonempty) {
         if ((st = build_graph(x)) != EMST_OK) return st;
         EMST_CUDA(x, cudaGraphLaunch(x->gexec, c.stream), "graph launch");
         if ((st = read_counters(x)) != EMST_OK) return st;
@@ -361,7 +365,7 @@ emst_status run_graph(emst_ctx* x)
     }
     c.finished = true;
     x->stage = 0;
-    if (c.n_roots > 1) {
+    if (c.n_roots > (uint32_t)c.n_nonempty) {
         if (c.round >= c.max_rounds) return set_err(x, EMST_ENOCONVERGE, "round cap reached");
         return set_err(x, EMST_ENOCONVERGE, "a round added no edge while several components remain");
     }
@@ -444,6 +448,16 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.lbp);
     emst::release(c.clb);
     emst::release(c.spl);
+    emst::release(c.d_off);
+    emst::release(c.d_foff);
+    emst::release(c.d_eoff);
+    emst::release(c.d_dims);
+    emst::release(c.stage);
+    emst::release(c.pcloud_in);
+    emst::release(c.pcloud);
+    emst::release(c.ncloud);
+    emst::release(c.bcursor);
+    emst::release(c.bedges);
     emst::release(c.cand);
     emst::release(c.cnt);
     emst::release(c.cur);
@@ -685,6 +699,101 @@ emst_status emst_solve(emst_ctx* x, const float* points, int64_t n, int dim, int
     if (n_edges) *n_edges = ne;
     if (uv) return emst_get_edges(x, uv, nullptr, n > 1 ? n - 1 : 0, nullptr);
     return EMST_OK;
+}
+
+emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* point_offsets, const int32_t* dims,
+                             int32_t n_clouds, int32_t* uv, double* lengths, int64_t* n_edges)
+{
+    if (!x) return EMST_EINVAL;
+    Ctx& c = x->c;
+    if (!points || !point_offsets || !dims || n_clouds < 1) return set_err(x, EMST_EINVAL, "bad batch arguments");
+    if (n_clouds > (1 << 16)) return set_err(x, EMST_EOVERFLOW, "at most 65536 clouds");
+    if (c.search_mode != 0 || c.cnns_warp)
+        return set_err(x, EMST_EINVAL, "batches run in the component search mode (search_mode 0)");
+    std::vector<int64_t> foff(n_clouds + 1), eoff(n_clouds + 1);
+    foff[0] = 0;
+    eoff[0] = 0;
+    int64_t nonempty = 0;
+    if (point_offsets[0] != 0) return set_err(x, EMST_EINVAL, "point_offsets[0] must be 0");
+    for (int i = 0; i < n_clouds; ++i) {
+        const int64_t m = point_offsets[i + 1] - point_offsets[i];
+        if (m < 0) return set_err(x, EMST_EINVAL, "point_offsets must not decrease");
+        if (dims[i] != 2 && dims[i] != 3) return set_err(x, EMST_EINVAL, "dims must be 2 or 3");
+        foff[i + 1] = foff[i] + m * dims[i];
+        eoff[i + 1] = eoff[i] + (m > 0 ? m - 1 : 0);
+        nonempty += m > 0;
+    }
+    const int64_t n = point_offsets[n_clouds];
+    if (n >= (int64_t)0x7fffffff) return set_err(x, EMST_EOVERFLOW, "total points must be < 2^31 - 1");
+    EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
+    if (n_edges) *n_edges = eoff[n_clouds];
+    if (n == 0) {
+        for (int i = 0; lengths && i < n_clouds; ++i) lengths[i] = 0.0;
+        return EMST_OK;
+    }
+    EMST_CUDA(x, emst::ensure(c.in_own, (size_t)foff[n_clouds]), "alloc points");
+    EMST_CUDA(x, emst::ensure(c.d_off, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, emst::ensure(c.d_foff, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, emst::ensure(c.d_eoff, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, emst::ensure(c.d_dims, (size_t)n_clouds), "alloc");
+    EMST_CUDA(x, emst::ensure(c.dlen, (size_t)n_clouds), "alloc");
+    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)2 * (eoff[n_clouds] > 0 ? eoff[n_clouds] : 1)), "alloc");
+    cudaStream_t s = c.stream;
+    EMST_CUDA(x, cudaMemcpyAsync(c.in_own.p, points, sizeof(float) * foff[n_clouds], cudaMemcpyHostToDevice, s),
+              "upload");
+    EMST_CUDA(x, cudaMemcpyAsync(c.d_off.p, point_offsets, sizeof(int64_t) * (n_clouds + 1), cudaMemcpyHostToDevice, s),
+              "upload");
+    EMST_CUDA(x, cudaMemcpyAsync(c.d_foff.p, foff.data(), sizeof(int64_t) * (n_clouds + 1), cudaMemcpyHostToDevice, s),
+              "upload");
+    EMST_CUDA(x, cudaMemcpyAsync(c.d_eoff.p, eoff.data(), sizeof(int64_t) * (n_clouds + 1), cudaMemcpyHostToDevice, s),
+              "upload");
+    EMST_CUDA(x, cudaMemcpyAsync(c.d_dims.p, dims, sizeof(int32_t) * n_clouds, cudaMemcpyHostToDevice, s), "upload");
+    c.in = c.in_own.p;
+    c.n = n;
+    c.dim = 3;  // 2D clouds carry z = 0 (fma(0, 0, r) == r keeps their distances 2D)
+    c.K = 24;
+    c.n_clouds = n_clouds;
+    c.n_nonempty = nonempty;
+    std::memset(c.hctr, 0, sizeof(emst::DevCounters));
+    c.hctr->n_act = (uint32_t)n;
+    c.hctr->n_roots = (uint32_t)n;
+    c.hctr->n_target = (uint32_t)nonempty;
+    EMST_CUDA(x, cudaMemcpyAsync(c.ctr.p, c.hctr, sizeof(emst::DevCounters), cudaMemcpyHostToDevice, s), "counters");
+    c.launches = 0;
+    c.nns_launches = 0;
+    for (double& v : x->ms) v = 0.0;
+    if (c.profile) {
+        EMST_CUDA(x, emst::ensure(c.nstats, 5), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 5 * sizeof(unsigned long long), s), "stats");
+    }
+    {
+        Timed t(x, PH_GRID);
+        EMST_CUDA(x, emst::batch_grid_build(c), "batch grid build");
+        EMST_CUDA(x, emst::boruvka_init(c), "init");
+        EMST_CUDA(x, emst::cnns_init(c), "init");
+    }
+    c.round = 0;
+    c.finished = false;
+    c.n_edges = 0;
+    c.n_zero = 0;
+    c.cum_edges.clear();
+    c.phase = 1;
+    x->stage = 0;
+    x->last_edges = 0;
+    emst_status st = do_run(x);
+    if (st != EMST_OK) return st;
+    if ((int64_t)c.n_edges != eoff[n_clouds])
+        return set_err(x, EMST_ECUDA, "batch edge count mismatch: " + std::to_string(c.n_edges) + " edges, expected " +
+                                          std::to_string(eoff[n_clouds]) + " after " + std::to_string(c.round) +
+                                          " rounds, " + std::to_string(c.n_roots) + " components");
+    EMST_CUDA(x, emst::batch_output(c, x->tmp_i32.p, c.dlen.p), "batch output");
+    if (uv && eoff[n_clouds] > 0)
+        EMST_CUDA(x, cudaMemcpyAsync(uv, x->tmp_i32.p, sizeof(int32_t) * 2 * eoff[n_clouds], cudaMemcpyDeviceToHost, s),
+                  "download");
+    if (lengths)
+        EMST_CUDA(x, cudaMemcpyAsync(lengths, c.dlen.p, sizeof(double) * n_clouds, cudaMemcpyDeviceToHost, s),
+                  "download");
+    return read_counters(x);
 }
 
 emst_status emst_solve_device(emst_ctx* x, const float* d_points, int64_t n, int dim, int32_t* d_uv,

@@ -48,7 +48,7 @@ struct DevCounters {
     uint32_t rpar;        // which half of the 2n roots buffer holds the current roots
     int32_t round;        // rounds started (device copy, read by k_hook)
     uint32_t prev_edges;  // edge count at the end of the previous round
-    uint32_t pad;
+    uint32_t n_target;    // components left when done (1, or the number of non-empty clouds)
 };
 
 struct NormParams {
@@ -122,6 +122,16 @@ struct Ctx {
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
     DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
     DevBuf<float4> spl;              // per round: (x, y, z, component label) in leaf order
+
+    // batch of clouds (batch.cu)
+    int n_clouds = 0;                // 0: single cloud
+    int64_t n_nonempty = 1;          // components left at the end
+    DevBuf<int64_t> d_off, d_foff, d_eoff;  // per cloud: first point, first float, first output edge row
+    DevBuf<int32_t> d_dims;
+    DevBuf<float4> stage;            // rescaled points in input order before the sort
+    DevBuf<uint32_t> pcloud_in, pcloud;  // cloud of each point (input / leaf order)
+    DevBuf<uint32_t> ncloud;             // per node: (first cloud << 16) | last cloud of its points
+    DevBuf<uint32_t> bcursor, bedges;            // output scatter cursors, edges with global ids
     DevBuf<uint32_t> clb;            // per root: min lbp over its dirty points (float bits)
     DevBuf<unsigned long long> nstats;  // region search: leaf visits, node tests, candidates, warps
 
@@ -135,6 +145,10 @@ struct Ctx {
 
 // grid.cu
 cudaError_t grid_build(Ctx& c);
+cudaError_t leaf_tree(Ctx& c);
+// batch.cu
+cudaError_t batch_grid_build(Ctx& c);
+cudaError_t batch_output(Ctx& c, int32_t* d_uv, double* d_len);
 // nns.cu
 cudaError_t nns_full(Ctx& c);
 cudaError_t nns_recompute_zero(Ctx& c);
@@ -154,6 +168,7 @@ cudaError_t table_to_host_order(Ctx& c);
 cudaError_t cnns_init(Ctx& c);
 cudaError_t cnns_node_labels(Ctx& c);
 cudaError_t cnns_select(Ctx& c);
+cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out);
 
 template <typename T>
 cudaError_t ensure(DevBuf<T>& b, size_t n)

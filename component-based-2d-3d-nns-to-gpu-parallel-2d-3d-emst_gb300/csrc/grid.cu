@@ -323,8 +323,16 @@ cudaError_t grid_build(Ctx& c)
         k_gather<2><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
     else
         k_gather<3><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
-    k_leaf_boxes<<<blocks_for(c.L * 32, 256), 256, 0, s>>>(c.sp.p, n, c.nchunk, c.L, c.nlo.p, c.nhi.p, c.nid.p);
-    c.launches += 5;
+    c.launches += 4;
+    return leaf_tree(c);
+}
+
+// Leaf boxes (+ two smallest ids) and the implicit tree above them.
+cudaError_t leaf_tree(Ctx& c)
+{
+    cudaStream_t s = c.stream;
+    k_leaf_boxes<<<blocks_for(c.L * 32, 256), 256, 0, s>>>(c.sp.p, c.n, c.nchunk, c.L, c.nlo.p, c.nhi.p, c.nid.p);
+    c.launches++;
     for (int64_t h = c.L >> 1; h >= 1; h >>= 1) {
         k_tree_level<<<blocks_for(h, 256), 256, 0, s>>>(c.nlo.p, c.nhi.p, c.nid.p, h, h);
         c.launches++;

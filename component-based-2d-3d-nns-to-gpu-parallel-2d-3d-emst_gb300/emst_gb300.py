@@ -74,7 +74,7 @@ def lib():
             "emst_get_round_stats": [P, P, P, i64], "emst_get_region_table": [P, P, P, i64],
             "emst_get_rescaled": [P, P, P, i64], "emst_solve": [P, P, i64, I, P, P, P],
             "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
-            "emst_region_table_noalloc": [P, i64, I, P, P, P],
+            "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -231,6 +231,22 @@ class Emst:
                                    ctypes.byref(ln)))
         self.n, self.dim = pts.shape
         return ne.value, ln.value
+
+    def solve_batch(self, clouds):
+        """clouds: list of (n_i, dim_i) float32 arrays -> (list of (n_i-1, 2) int32 edges, lengths)."""
+        sizes = np.array([len(c) for c in clouds], np.int64)
+        dims = np.array([c.shape[1] for c in clouds], np.int32)
+        offs = np.zeros(len(clouds) + 1, np.int64)
+        offs[1:] = np.cumsum(sizes)
+        flat = np.ascontiguousarray(np.concatenate([np.ascontiguousarray(c, np.float32).ravel() for c in clouds]))
+        rows = int(np.maximum(sizes - 1, 0).sum())
+        uv = np.zeros((max(rows, 1), 2), np.int32)
+        lens = np.zeros(len(clouds), np.float64)
+        ne = ctypes.c_int64()
+        self._chk(lib().emst_solve_batch(self.h, _p(flat), _p(offs), _p(dims), len(clouds), _p(uv), _p(lens),
+                                         ctypes.byref(ne)))
+        eo = np.concatenate([[0], np.cumsum(np.maximum(sizes - 1, 0))])
+        return [uv[eo[i]:eo[i + 1]].copy() for i in range(len(clouds))], lens
 
     def solve_device(self, d_points, n, dim, d_uv, d_length):
         ne = ctypes.c_int64()

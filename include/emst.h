@@ -186,6 +186,17 @@ emst_status emst_get_rescaled(emst_ctx* ctx, float* out, double* unit_x, int64_t
 emst_status emst_solve(emst_ctx* ctx, const float* points, int64_t n, int dim, int32_t* uv, int64_t* n_edges,
                        double* length);
 
+/* Many independent clouds, 2D and 3D mixed, in one solve (one sort, one
+ * tree, one round loop): the batched form of CalculateurEMST::run.
+ * points: the clouds' AoS floats back to back (cloud i: n_i * dims[i]);
+ * point_offsets: n_clouds + 1 cumulative point counts (host);
+ * uv: sum of max(n_i - 1, 0) pairs, cloud i's edges first at row
+ *     sum_{j<i} max(n_j - 1, 0), local point ids (u < v);
+ * lengths: per cloud, as emst_evaluate.  Each cloud's edge set is the one
+ * emst_solve gives for that cloud alone.  Component search mode only. */
+emst_status emst_solve_batch(emst_ctx* ctx, const float* points, const int64_t* point_offsets, const int32_t* dims,
+                             int32_t n_clouds, int32_t* uv, double* lengths, int64_t* n_edges);
+
 /* Device buffers in and out (points n*dim floats; uv 2*(n-1) int32;
  * length one double), no host synchronisation except the per-round
  * termination read. */

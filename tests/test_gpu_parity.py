@@ -179,6 +179,50 @@ def test_graph_loop_matches_host_loop(gpu_lib, kind, dim, n):
     assert np.array_equal(out[0][3], out[1][3])
 
 
+def test_batch_equals_per_cloud_solves(gpu_lib):
+    """One batched solve of mixed 2D/3D clouds (sizes 0, 1, 2, small and large,
+    duplicates and clusters) gives, cloud by cloud, the edge set and length of
+    solving that cloud alone."""
+    rng = np.random.default_rng(5)
+    clouds = []
+    for i in range(40):
+        n = int(rng.choice([0, 1, 2, 3, 50, 500, 3000, 20000]))
+        dim = int(rng.choice([2, 3]))
+        kind = KINDS[i % len(KINDS)]
+        clouds.append(family(kind, n, dim, 300 + i) if n > 0 else np.zeros((0, dim), np.float32))
+    with gpu_lib.Emst() as e:
+        uvs, lens = e.solve_batch(clouds)
+    for pts, uv, ln in zip(clouds, uvs, lens):
+        if len(pts) < 2:
+            assert len(uv) == 0 and ln == 0.0
+            continue
+        with gpu_lib.Emst() as e:
+            ref_uv, ref_len = e.solve(pts)
+        assert np.array_equal(_canon(uv), _canon(ref_uv))
+        assert ln == pytest.approx(ref_len, rel=1e-9)
+
+
+def test_batch_workload_512_clouds_vs_oracle(gpu_lib):
+    """The 512-cloud workload (sizes log-uniform 1e3..1e5, half 2D half 3D,
+    uniform or 8-cluster): every cloud against the oracle on a sample, all
+    against per-cloud solves."""
+    clouds = W.batch_clouds()
+    with gpu_lib.Emst() as e:
+        uvs, lens = e.solve_batch(clouds)
+    assert len(uvs) == 512
+    for i in range(0, 512, 37):
+        if len(clouds[i]) > 30000:
+            continue
+        sp, _, _, _ = O.rescale(clouds[i])
+        ref = O.emst(sp, "faithful")
+        assert np.array_equal(_canon(uvs[i]), _canon(ref.edges))
+        assert lens[i] == pytest.approx(O.length(clouds[i], ref.edges), rel=1e-9)
+    with gpu_lib.Emst() as e:
+        for i in range(1, 512, 29):
+            ref_uv, _ = e.solve(clouds[i])
+            assert np.array_equal(_canon(uvs[i]), _canon(ref_uv))
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
