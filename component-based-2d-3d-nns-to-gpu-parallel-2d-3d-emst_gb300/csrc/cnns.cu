@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(256, 4)
                 const float own = __uint_as_float(labp);
                 // a leaf straddling clouds: check every candidate's cloud
                 bool mixed = false;
-                if (CL) {
+                if constexpr (CL) {
                     const uint32_t r = __ldg(&ncloud[L + leaf]);
                     mixed = (r >> 16) != (r & 0xffffu);
                 }
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(256, 4)
                 const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
                 if (lo.x > hi.x) return INFINITY;
                 if (__ldg(&nlab[node]) == labp) return INFINITY;  // all in the query's component
-                if (CL) {
+                if constexpr (CL) {
                     // (first cloud << 16) | last cloud of the node's points
                     const uint32_t r = __ldg(&ncloud[node]);
                     if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;  // all in other clouds
@@ -426,40 +426,66 @@ __global__ void __launch_bounds__(256, 4)
                 return d2_of<D>(gx, gy, gz);
             };
 
+            // Own leaf first, then bottom-up: the sibling subtree of each
+            // ancestor, nearest levels first, each searched depth-first with
+            // the nearer child next.  Sibling addresses are known up front,
+            // so no descent from the root is needed.
             const uint32_t own = me >> 5;
             if (__ldg(&nlab[L + own]) != labp) scan_leaf(own);
             uint32_t stack[kTStack];
-            int top = 0;
-            stack[top++] = 1u;
-            while (top > 0) {
-                const uint32_t node = stack[--top];
+            for (uint32_t v = L + own; v > 1; v >>= 1) {
+                const uint32_t sib = v ^ 1u;
                 ++st_nodes;
-                if (node >= L) {
-                    if (node - L == own) continue;
-                    // bound re-checked: bd may have shrunk since the push
-                    const float lb = node_lb(node);
-                    if (!(lb < INFINITY) || lb > bd) continue;
-                    if (lb > cb) {
-                        cut = fminf(cut, lb);
-                        continue;
-                    }
-                    scan_leaf(node - L);
-                    const uint64_t k = __ldcg(&ckey[labp]);
-                    cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+                const float ls = node_lb(sib);
+                if (!(ls < INFINITY)) continue;
+                if (ls > fminf(bd, cb)) {
+                    if (ls <= bd) cut = fminf(cut, ls);
                     continue;
                 }
-                const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                const float l0 = node_lb(c0), l1 = node_lb(c1);
-                const float lim = fminf(bd, cb);
-                // push the farther child first so the nearer one is searched next
-                const bool near0 = l0 <= l1;
-                const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
-                const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
-                if (top + 2 > kTStack) break;  // cannot happen for trees of depth < 46
-                if (lf < INFINITY && lf <= lim) stack[top++] = cf;
-                else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
-                if (ln < INFINITY && ln <= lim) stack[top++] = cn;
-                else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
+                int top = 0;
+                stack[top++] = sib;
+                while (top > 0) {
+                    // Traverse until this lane holds a leaf to scan, then scan
+                    // it together with the other lanes that hold one: leaf
+                    // scans of different lanes run side by side instead of
+                    // alternating with node expansions.
+                    uint32_t leaf = kNone;
+                    while (top > 0) {
+                        const uint32_t node = stack[--top];
+                        ++st_nodes;
+                        if (node >= L) {
+                            // bound re-checked: bd may have shrunk since the push
+                            const float lb = node_lb(node);
+                            if (!(lb < INFINITY) || lb > bd) continue;
+                            if (lb > cb) {
+                                cut = fminf(cut, lb);
+                                continue;
+                            }
+                            leaf = node - L;
+                            break;
+                        }
+                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                        const float l0 = node_lb(c0), l1 = node_lb(c1);
+                        const float lim = fminf(bd, cb);
+                        // push the farther child first so the nearer one is searched next
+                        const bool near0 = l0 <= l1;
+                        const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
+                        const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
+                        if (top + 2 > kTStack) {  // cannot happen for trees of depth < 46
+                            top = 0;
+                            break;
+                        }
+                        if (lf < INFINITY && lf <= lim) stack[top++] = cf;
+                        else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
+                        if (ln < INFINITY && ln <= lim) stack[top++] = cn;
+                        else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
+                    }
+                    if (leaf != kNone) {
+                        scan_leaf(leaf);
+                        const uint64_t k = __ldcg(&ckey[labp]);
+                        cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+                    }
+                }
             }
             const bool exact = bs >= 0 && bd < cut;
             lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
