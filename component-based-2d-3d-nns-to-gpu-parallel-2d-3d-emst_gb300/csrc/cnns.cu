@@ -27,6 +27,9 @@
 // and with it every round's edge set -- equals the static-table method's.
 #include <climits>
 
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
 #include "emst_ctx.h"
 #include "emst_device.cuh"
 
@@ -117,8 +120,8 @@ __device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* l
 // component's minimum bound clb.
 __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, const uint32_t* __restrict__ selq,
                         const uint64_t* __restrict__ selkey, const float* __restrict__ lbp,
-                        uint64_t* __restrict__ ckey, uint32_t* __restrict__ clb, uint32_t* __restrict__ dirty,
-                        uint32_t* __restrict__ n_dirty, uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov)
+                        uint64_t* __restrict__ ckey, uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag,
+                        uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov)
 {
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
@@ -140,7 +143,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, const uint
                 if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
             }
         }
-        warp_append(is_dirty, p, dirty, n_dirty);
+        if (p < n) dflag[p] = is_dirty ? 1 : 0;
         warp_append(record, p, prov, n_prov);
     }
 }
@@ -331,7 +334,7 @@ __global__ void __launch_bounds__(256, 4)
              const uint32_t* __restrict__ n_list, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
              uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
              uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
-             uint32_t* __restrict__ defer, uint32_t* __restrict__ n_defer, const uint32_t* __restrict__ pcloud,
+             unsigned char* __restrict__ dflag, const uint32_t* __restrict__ pcloud,
              const uint32_t* __restrict__ ncloud, unsigned long long* __restrict__ stats)
 {
     constexpr int kTStack = 48;
@@ -354,8 +357,8 @@ __global__ void __launch_bounds__(256, 4)
                 deferred = true;
             }
         }
-        __syncwarp();
-        warp_append(deferred, me, defer, n_defer);
+        // second-pass flags, compacted in leaf order after the first pass
+        if (listed && pass == 1) dflag[me] = deferred ? 1 : 0;
 
         bool record = false;
         uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
@@ -594,6 +597,12 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.clb, n)) != cudaSuccess) return e;
     if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
     if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
+    if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
+    size_t tb = 0;
+    if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
+                                        &c.ctr.p->n_dirty, (int)n, c.stream)) != cudaSuccess)
+        return e;
+    if ((e = ensure(c.sel_tmp, tb)) != cudaSuccess) return e;
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
     cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
@@ -607,7 +616,13 @@ cudaError_t cnns_select(Ctx& c)
 {
     DevCounters* d = c.ctr.p;  // n_dirty, n_dirty2, n_prov were zeroed by the round tick
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
-                                                  c.clb.p, c.dirty.p, &d->n_dirty, c.prov.p, &d->n_prov);
+                                                  c.clb.p, c.dflag.p, c.prov.p, &d->n_prov);
+    // dirty points in leaf order: a warp's 32 queries are neighbours, so their
+    // traversals share nodes and cache lines
+    size_t tb = c.sel_tmp.cap;
+    cudaError_t e = cub::DeviceSelect::Flagged(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p,
+                                               c.dirty.p, &d->n_dirty, (int)c.n, c.stream);
+    if (e != cudaSuccess) return e;
     constexpr int WPB = 4;
     const unsigned blocks = (unsigned)std::min<int64_t>((c.n + 32 * WPB - 1) / (32 * WPB), 152 * 32);
     unsigned long long* st = c.profile ? c.nstats.p : nullptr;
@@ -633,7 +648,13 @@ cudaError_t cnns_select(Ctx& c)
                                    : (pc ? k_cnns_t<3, true> : k_cnns_t<3, false>);
             kern<<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L,
                                            list, cnt, c.lab.p, c.ckey.p, c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,
-                                           c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2, pc, nc, st);
+                                           c.lbp.p, c.clb.p, pass, c.dflag.p, pc, nc, st);
+            if (pass == 1) {
+                size_t tbytes = c.sel_tmp.cap;
+                cudaError_t e2 = cub::DeviceSelect::Flagged(c.sel_tmp.p, tbytes, thrust::counting_iterator<uint32_t>(0),
+                                                            c.dflag.p, c.dirty2.p, &d->n_dirty2, (int)c.n, c.stream);
+                if (e2 != cudaSuccess) return e2;
+            }
         }
         c.nns_launches++;
     }

@@ -303,7 +303,7 @@ emst_status build_graph(emst_ctx* x)
     Ctx& c = x->c;
     std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
                                     c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
-                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p,
+                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p, c.dflag.p, c.sel_tmp.p,
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
@@ -445,6 +445,8 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.nlab);
     emst::release(c.dirty);
     emst::release(c.dirty2);
+    emst::release(c.dflag);
+    emst::release(c.sel_tmp);
     emst::release(c.lbp);
     emst::release(c.clb);
     emst::release(c.spl);

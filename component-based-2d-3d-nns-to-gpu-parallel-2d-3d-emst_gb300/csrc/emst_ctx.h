@@ -120,6 +120,7 @@ struct Ctx {
     bool use_graph = true;    // component search: run the round loop as one CUDA graph
     DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
+    DevBuf<unsigned char> dflag, sel_tmp;  // per point: dirty flag; compaction scratch
     DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
     DevBuf<float4> spl;              // per round: (x, y, z, component label) in leaf order
 
