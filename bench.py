@@ -202,6 +202,7 @@ def main():
     ap.add_argument("--mode", type=int, default=0, help="0: component search, 1: static region table")
     ap.add_argument("--no-static", action="store_true", help="skip the one-step static-table comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-cloud batch comparison")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -235,7 +236,16 @@ def main():
     # per-phase CUDA events) gives the phase split and the kernel times
     ctx = E.Emst(device=local, search_mode=args.mode)
     ctx.set_stream(stream.cuda_stream)
-    pctx = E.Emst(device=local, profile=True, search_mode=args.mode)
+    # launch shape of the component search: the autotuner times each shape on
+    # this workload (before the timed region) and keeps the fastest
+    shape, shape_ms = 0, None
+    if args.mode == 0 and not args.no_autotune:
+        shape, shape_ms = ctx.autotune(pts)
+    _, sh_threads, sh_blocks = E.search_shapes()
+    sh = shape if shape else 2  # library default: entry 2 of the table
+    launch_shape = {"threads": int(sh_threads[sh - 1]), "min_blocks_per_sm": int(sh_blocks[sh - 1]),
+                    "search_shape": sh, "autotuned_ms": None if shape_ms is None else [round(float(v), 3) for v in shape_ms]}
+    pctx = E.Emst(device=local, profile=True, search_mode=args.mode, search_shape=shape)
     pctx.set_stream(stream.cuda_stream)
 
     def step():
@@ -358,6 +368,7 @@ def main():
                            "search": {0: "component, thread per query", 1: "static region table",
                                       2: "component, warp per 32 queries"}[args.mode],
                            "l2": "512 MB buffer written between timed steps; working set > 129 MB L2",
+                           "launch_shape": launch_shape,
                            "parallelism": "replicas" if world > 1 else "single"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "kernel": kernel,

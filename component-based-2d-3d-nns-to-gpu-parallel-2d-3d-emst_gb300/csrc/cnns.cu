@@ -30,17 +30,12 @@
 #include <cub/device/device_select.cuh>
 #include <thrust/iterator/counting_iterator.h>
 
-#include "emst_ctx.h"
-#include "emst_device.cuh"
+#include "cnns_search.cuh"
 
 namespace emst {
 
 namespace {
 
-constexpr unsigned kFull = 0xffffffffu;
-constexpr uint32_t kMixed = 0xffffffffu;
-constexpr uint32_t kEmpty = 0xfffffffeu;
-constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kStack = 64;
 constexpr int kLeavesPerBlock = 1024;
 
@@ -99,20 +94,6 @@ __global__ void __launch_bounds__(1024) k_node_labels_top(uint32_t top, uint32_t
             nlab[h + t] = merge_label(nlab[2 * (h + t)], nlab[2 * (h + t) + 1]);
         __syncthreads();
     }
-}
-
-// Warp-aggregated append of `val` to list[] through counter *cnt.
-__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* list, uint32_t* cnt)
-{
-    const unsigned act = __activemask();
-    const unsigned m = __ballot_sync(act, pred);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(cnt, (uint32_t)__popc(m));
-    base = __shfl_sync(act, base, leader);
-    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
 // Points whose previous partner is still outside their component re-submit
@@ -320,216 +301,6 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 }
 
-// One thread per dirty point, each with its own traversal order: its own
-// leaf first, then a depth-first walk from the root pushing the nearer child
-// last, so every query sees good bounds early (queries of later rounds are
-// sparse, and one warp-wide order would serve only some of them).
-// CL: batched clouds (pcloud / ncloud given); a candidate must share the
-// query's cloud.
-template <int D, bool CL>
-__global__ void __launch_bounds__(256, 4)
-    k_cnns_t(const float4* __restrict__ spl, const uint32_t* __restrict__ perm, const float4* __restrict__ nlo,
-             const float4* __restrict__ nhi, const uint32_t* __restrict__ nlab, uint32_t n, uint32_t L,
-             const uint32_t* __restrict__ list,
-             const uint32_t* __restrict__ n_list, const uint32_t* __restrict__ lab, uint64_t* __restrict__ ckey,
-             uint32_t* __restrict__ selq, uint64_t* __restrict__ selkey, uint32_t* __restrict__ prov,
-             uint32_t* __restrict__ n_prov, float* __restrict__ lbp, const uint32_t* __restrict__ clb, int pass,
-             unsigned char* __restrict__ dflag, const uint32_t* __restrict__ pcloud,
-             const uint32_t* __restrict__ ncloud, unsigned long long* __restrict__ stats)
-{
-    constexpr int kTStack = 48;
-    const uint32_t total = *n_list;
-    for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
-        const uint32_t qi = base0 + threadIdx.x;
-        const bool listed = qi < total;
-        const uint32_t me = listed ? list[qi] : 0u;
-        const uint32_t labp = listed ? lab[me] : kEmpty;
-        const float lb0 = listed ? lbp[me] : 0.f;
-        bool valid = listed, deferred = false;
-        float cb = INFINITY;
-        if (listed) {
-            const uint64_t k = __ldcg(&ckey[labp]);
-            cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
-            if (lb0 > cb) {
-                valid = false;  // cannot hold its component's minimum this round
-            } else if (pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
-                valid = false;  // not among its component's most promising points: second pass
-                deferred = true;
-            }
-        }
-        // second-pass flags, compacted in leaf order after the first pass
-        if (listed && pass == 1) dflag[me] = deferred ? 1 : 0;
-
-        bool record = false;
-        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
-        if (valid) {
-            const float4 P = spl[me];
-            const int op = (int)perm[me];
-            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;  // the query's cloud (batches)
-            float bd = INFINITY, cut = INFINITY;
-            int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
-            int bs = -1;  // leaf position of the best
-
-            // spl holds (x, y, z, label bits); input ids are needed only to
-            // break exact d2 ties and for the final key.
-            auto scan_leaf = [&](uint32_t leaf) {
-                const uint32_t b = leaf * 32;
-                if (b >= n) return;  // padding leaf (never reached: its bound is +inf)
-                const uint32_t m = min(32u, n - b);
-                ++st_leaves;
-                st_cands += m;
-                const float own = __uint_as_float(labp);
-                // a leaf straddling clouds: check every candidate's cloud
-                bool mixed = false;
-                if constexpr (CL) {
-                    const uint32_t r = __ldg(&ncloud[L + leaf]);
-                    mixed = (r >> 16) != (r & 0xffffu);
-                }
-                for (uint32_t j = 0; j < m; j += 4) {
-                    float4 c[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, own);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        if (__float_as_uint(c[k].w) == labp) continue;
-                        if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
-                        const float d2 =
-                            d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z));
-                        if (d2 < bd) {
-                            bd = d2;
-                            bs = (int)(b + j + k);
-                            bo = -1;
-                        } else if (d2 == bd) {
-                            const int oq = (int)__ldg(&perm[b + j + k]);
-                            if (bo < 0) bo = (int)__ldg(&perm[bs]);
-                            if (oq < bo) {
-                                bo = oq;
-                                bs = (int)(b + j + k);
-                            }
-                        }
-                    }
-                }
-            };
-            // lower bound of d2 over a node's box, or +inf when the node cannot
-            // help (empty, all in the query's component, all in another cloud);
-            // +inf is tested explicitly: best and shared bound may be +inf too
-            auto node_lb = [&](uint32_t node) -> float {
-                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
-                if (lo.x > hi.x) return INFINITY;
-                if (__ldg(&nlab[node]) == labp) return INFINITY;  // all in the query's component
-                if constexpr (CL) {
-                    // (first cloud << 16) | last cloud of the node's points
-                    const uint32_t r = __ldg(&ncloud[node]);
-                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;  // all in other clouds
-                }
-                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
-                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
-                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
-                return d2_of<D>(gx, gy, gz);
-            };
-
-            // Own leaf first, then bottom-up: the sibling subtree of each
-            // ancestor, nearest levels first, each searched depth-first with
-            // the nearer child next.  Sibling addresses are known up front,
-            // so no descent from the root is needed.
-            const uint32_t own = me >> 5;
-            if (__ldg(&nlab[L + own]) != labp) scan_leaf(own);
-            uint32_t stack[kTStack];
-            for (uint32_t v = L + own; v > 1; v >>= 1) {
-                const uint32_t sib = v ^ 1u;
-                ++st_nodes;
-                const float ls = node_lb(sib);
-                if (!(ls < INFINITY)) continue;
-                if (ls > fminf(bd, cb)) {
-                    if (ls <= bd) cut = fminf(cut, ls);
-                    continue;
-                }
-                int top = 0;
-                stack[top++] = sib;
-                while (top > 0) {
-                    // Traverse until this lane holds a leaf to scan, then scan
-                    // it together with the other lanes that hold one: leaf
-                    // scans of different lanes run side by side instead of
-                    // alternating with node expansions.
-                    uint32_t leaf = kNone;
-                    while (top > 0) {
-                        const uint32_t node = stack[--top];
-                        ++st_nodes;
-                        if (node >= L) {
-                            // bound re-checked: bd may have shrunk since the push
-                            const float lb = node_lb(node);
-                            if (!(lb < INFINITY) || lb > bd) continue;
-                            if (lb > cb) {
-                                cut = fminf(cut, lb);
-                                continue;
-                            }
-                            leaf = node - L;
-                            break;
-                        }
-                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                        const float l0 = node_lb(c0), l1 = node_lb(c1);
-                        const float lim = fminf(bd, cb);
-                        // push the farther child first so the nearer one is searched next
-                        const bool near0 = l0 <= l1;
-                        const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
-                        const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
-                        if (top + 2 > kTStack) {  // cannot happen for trees of depth < 46
-                            top = 0;
-                            break;
-                        }
-                        if (lf < INFINITY && lf <= lim) stack[top++] = cf;
-                        else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
-                        if (ln < INFINITY && ln <= lim) stack[top++] = cn;
-                        else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
-                    }
-                    if (leaf != kNone) {
-                        scan_leaf(leaf);
-                        const uint64_t k = __ldcg(&ckey[labp]);
-                        cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
-                    }
-                }
-            }
-            const bool exact = bs >= 0 && bd < cut;
-            lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
-            if (bs >= 0) {
-                if (bo < 0) bo = (int)__ldg(&perm[bs]);
-                const uint32_t mn = (uint32_t)min(op, bo);
-                const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
-                selq[me] = exact ? (uint32_t)bs : kNone;
-                selkey[me] = key;
-                if (key <= __ldcg(&ckey[labp])) {
-                    const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
-                    record = old >= key;
-                }
-            } else {
-                selq[me] = kNone;
-            }
-        }
-        // Reconverge the warp before its next 32 queries: without this the
-        // lanes of a diverged warp drift into different iterations and the
-        // next traversals run with a fraction of the warp active.
-        __syncwarp();
-        warp_append(record, me, prov, n_prov);
-        if (stats) {
-            unsigned long long a = st_leaves, b = st_nodes, c = st_cands, q = valid ? 1ull : 0ull;
-            for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_xor_sync(kFull, a, o);
-                b += __shfl_xor_sync(kFull, b, o);
-                c += __shfl_xor_sync(kFull, c, o);
-                q += __shfl_xor_sync(kFull, q, o);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(&stats[0], a);
-                atomicAdd(&stats[1], b);
-                atomicAdd(&stats[2], c);
-                atomicAdd(&stats[3], 1ull);
-                atomicAdd(&stats[4], q);
-            }
-        }
-    }
-}
-
 // Per round: points in leaf order with their current component label.
 __global__ void k_pack_spl(uint32_t n, const float4* __restrict__ sp, const uint32_t* __restrict__ lab,
                            float4* __restrict__ spl)
@@ -643,12 +414,13 @@ cudaError_t cnns_select(Ctx& c)
                     c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2,
                     st);
         } else {
-            const unsigned tb = list_grid(c.n);
-            auto kern = c.dim == 2 ? (pc ? k_cnns_t<2, true> : k_cnns_t<2, false>)
-                                   : (pc ? k_cnns_t<3, true> : k_cnns_t<3, false>);
-            kern<<<tb, 256, 0, c.stream>>>(c.spl.p, c.perm.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L,
-                                           list, cnt, c.lab.p, c.ckey.p, c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,
-                                           c.lbp.p, c.clb.p, pass, c.dflag.p, pc, nc, st);
+            CnnsArgs a{c.spl.p, c.perm.p, c.nlo.p,  c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
+                       cnt,     c.lab.p,  c.ckey.p, c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p,
+                       c.clb.p, pass,     c.dflag.p, pc,     nc,        st};
+            const int shape = search_shape_of(c);
+            cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, shape, c.sms, c.stream)
+                                        : launch_cnns_t3(a, pc != nullptr, shape, c.sms, c.stream);
+            if (e1 != cudaSuccess) return e1;
             if (pass == 1) {
                 size_t tbytes = c.sel_tmp.cap;
                 cudaError_t e2 = cub::DeviceSelect::Flagged(c.sel_tmp.p, tbytes, thrust::counting_iterator<uint32_t>(0),

@@ -1,0 +1,290 @@
+// cnns_search.cuh -- the thread-per-query component search kernel, shared by
+// the per-dimension translation units that instantiate it for every launch
+// shape of the table (cnns_t2.cu, cnns_t3.cu).
+#pragma once
+#include <climits>
+
+#include "emst_ctx.h"
+#include "emst_device.cuh"
+
+namespace emst {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kMixed = 0xffffffffu;
+constexpr uint32_t kEmpty = 0xfffffffeu;
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Warp-aggregated append of `val` to list[] through counter *cnt.
+__device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* list, uint32_t* cnt)
+{
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (uint32_t)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
+}
+
+// One thread per dirty point, each with its own traversal order: its own
+// leaf first, then a depth-first walk from the root pushing the nearer child
+// last, so every query sees good bounds early (queries of later rounds are
+// sparse, and one warp-wide order would serve only some of them).
+// CL: batched clouds (pcloud / ncloud given); a candidate must share the
+// query's cloud.
+// TPB threads per block, at least MINB blocks resident per SM (the launch
+// shape; kSearchShapes lists the instantiated pairs).
+template <int D, bool CL, int TPB, int MINB>
+__global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
+{
+    const float4* __restrict__ spl = a.spl;
+    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ nlo = a.nlo;
+    const float4* __restrict__ nhi = a.nhi;
+    const uint32_t* __restrict__ nlab = a.nlab;
+    const uint32_t n = a.n, L = a.L;
+    const uint32_t* __restrict__ list = a.list;
+    const uint32_t* __restrict__ n_list = a.n_list;
+    const uint32_t* __restrict__ lab = a.lab;
+    uint64_t* __restrict__ ckey = a.ckey;
+    uint32_t* __restrict__ selq = a.selq;
+    uint64_t* __restrict__ selkey = a.selkey;
+    uint32_t* __restrict__ prov = a.prov;
+    uint32_t* __restrict__ n_prov = a.n_prov;
+    float* __restrict__ lbp = a.lbp;
+    const uint32_t* __restrict__ clb = a.clb;
+    const int pass = a.pass;
+    unsigned char* __restrict__ dflag = a.dflag;
+    const uint32_t* __restrict__ pcloud = a.pcloud;
+    const uint32_t* __restrict__ ncloud = a.ncloud;
+    unsigned long long* __restrict__ stats = a.stats;
+    constexpr int kTStack = 48;
+    const uint32_t total = *n_list;
+    for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
+        const uint32_t qi = base0 + threadIdx.x;
+        const bool listed = qi < total;
+        const uint32_t me = listed ? list[qi] : 0u;
+        const uint32_t labp = listed ? lab[me] : kEmpty;
+        const float lb0 = listed ? lbp[me] : 0.f;
+        bool valid = listed, deferred = false;
+        float cb = INFINITY;
+        if (listed) {
+            const uint64_t k = __ldcg(&ckey[labp]);
+            cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+            if (lb0 > cb) {
+                valid = false;  // cannot hold its component's minimum this round
+            } else if (pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
+                valid = false;  // not among its component's most promising points: second pass
+                deferred = true;
+            }
+        }
+        // second-pass flags, compacted in leaf order after the first pass
+        if (listed && pass == 1) dflag[me] = deferred ? 1 : 0;
+
+        bool record = false;
+        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
+        if (valid) {
+            const float4 P = spl[me];
+            const int op = (int)perm[me];
+            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;  // the query's cloud (batches)
+            float bd = INFINITY, cut = INFINITY;
+            int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
+            int bs = -1;  // leaf position of the best
+
+            // spl holds (x, y, z, label bits); input ids are needed only to
+            // break exact d2 ties and for the final key.
+            auto scan_leaf = [&](uint32_t leaf) {
+                const uint32_t b = leaf * 32;
+                if (b >= n) return;  // padding leaf (never reached: its bound is +inf)
+                const uint32_t m = min(32u, n - b);
+                ++st_leaves;
+                st_cands += m;
+                const float own = __uint_as_float(labp);
+                // a leaf straddling clouds: check every candidate's cloud
+                bool mixed = false;
+                if constexpr (CL) {
+                    const uint32_t r = __ldg(&ncloud[L + leaf]);
+                    mixed = (r >> 16) != (r & 0xffffu);
+                }
+                for (uint32_t j = 0; j < m; j += 4) {
+                    float4 c[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, own);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (__float_as_uint(c[k].w) == labp) continue;
+                        if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
+                        const float d2 =
+                            d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z));
+                        if (d2 < bd) {
+                            bd = d2;
+                            bs = (int)(b + j + k);
+                            bo = -1;
+                        } else if (d2 == bd) {
+                            const int oq = (int)__ldg(&perm[b + j + k]);
+                            if (bo < 0) bo = (int)__ldg(&perm[bs]);
+                            if (oq < bo) {
+                                bo = oq;
+                                bs = (int)(b + j + k);
+                            }
+                        }
+                    }
+                }
+            };
+            // lower bound of d2 over a node's box, or +inf when the node cannot
+            // help (empty, all in the query's component, all in another cloud);
+            // +inf is tested explicitly: best and shared bound may be +inf too
+            auto node_lb = [&](uint32_t node) -> float {
+                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                if (lo.x > hi.x) return INFINITY;
+                if (__ldg(&nlab[node]) == labp) return INFINITY;  // all in the query's component
+                if constexpr (CL) {
+                    // (first cloud << 16) | last cloud of the node's points
+                    const uint32_t r = __ldg(&ncloud[node]);
+                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;  // all in other clouds
+                }
+                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+                return d2_of<D>(gx, gy, gz);
+            };
+
+            // Own leaf first, then bottom-up: the sibling subtree of each
+            // ancestor, nearest levels first, each searched depth-first with
+            // the nearer child next.  Sibling addresses are known up front,
+            // so no descent from the root is needed.
+            const uint32_t own = me >> 5;
+            if (__ldg(&nlab[L + own]) != labp) scan_leaf(own);
+            uint32_t stack[kTStack];
+            for (uint32_t v = L + own; v > 1; v >>= 1) {
+                const uint32_t sib = v ^ 1u;
+                ++st_nodes;
+                const float ls = node_lb(sib);
+                if (!(ls < INFINITY)) continue;
+                if (ls > fminf(bd, cb)) {
+                    if (ls <= bd) cut = fminf(cut, ls);
+                    continue;
+                }
+                int top = 0;
+                stack[top++] = sib;
+                while (top > 0) {
+                    // Traverse until this lane holds a leaf to scan, then scan
+                    // it together with the other lanes that hold one: leaf
+                    // scans of different lanes run side by side instead of
+                    // alternating with node expansions.
+                    uint32_t leaf = kNone;
+                    while (top > 0) {
+                        const uint32_t node = stack[--top];
+                        ++st_nodes;
+                        if (node >= L) {
+                            // bound re-checked: bd may have shrunk since the push
+                            const float lb = node_lb(node);
+                            if (!(lb < INFINITY) || lb > bd) continue;
+                            if (lb > cb) {
+                                cut = fminf(cut, lb);
+                                continue;
+                            }
+                            leaf = node - L;
+                            break;
+                        }
+                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                        const float l0 = node_lb(c0), l1 = node_lb(c1);
+                        const float lim = fminf(bd, cb);
+                        // push the farther child first so the nearer one is searched next
+                        const bool near0 = l0 <= l1;
+                        const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
+                        const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
+                        if (top + 2 > kTStack) {  // cannot happen for trees of depth < 46
+                            top = 0;
+                            break;
+                        }
+                        if (lf < INFINITY && lf <= lim) stack[top++] = cf;
+                        else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
+                        if (ln < INFINITY && ln <= lim) stack[top++] = cn;
+                        else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
+                    }
+                    if (leaf != kNone) {
+                        scan_leaf(leaf);
+                        const uint64_t k = __ldcg(&ckey[labp]);
+                        cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+                    }
+                }
+            }
+            const bool exact = bs >= 0 && bd < cut;
+            lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
+            if (bs >= 0) {
+                if (bo < 0) bo = (int)__ldg(&perm[bs]);
+                const uint32_t mn = (uint32_t)min(op, bo);
+                const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
+                selq[me] = exact ? (uint32_t)bs : kNone;
+                selkey[me] = key;
+                if (key <= __ldcg(&ckey[labp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                selq[me] = kNone;
+            }
+        }
+        // Reconverge the warp before its next 32 queries: without this the
+        // lanes of a diverged warp drift into different iterations and the
+        // next traversals run with a fraction of the warp active.
+        __syncwarp();
+        warp_append(record, me, prov, n_prov);
+        if (stats) {
+            unsigned long long a = st_leaves, b = st_nodes, c = st_cands, q = valid ? 1ull : 0ull;
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(kFull, a, o);
+                b += __shfl_xor_sync(kFull, b, o);
+                c += __shfl_xor_sync(kFull, c, o);
+                q += __shfl_xor_sync(kFull, q, o);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&stats[0], a);
+                atomicAdd(&stats[1], b);
+                atomicAdd(&stats[2], c);
+                atomicAdd(&stats[3], 1ull);
+                atomicAdd(&stats[4], q);
+            }
+        }
+    }
+}
+
+
+// Launch of one shape; the grid covers the list's upper bound `a.n` with at
+// most four waves of resident blocks (the kernel strides over the rest).
+template <int D, bool CL, int I>
+void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
+{
+    constexpr int T = kSearchShapes[I].threads, M = kSearchShapes[I].min_blocks;
+    uint64_t b = ((uint64_t)a.n + T - 1) / T;
+    const uint64_t cap = (uint64_t)sms * M * 4;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    k_cnns_t<D, CL, T, M><<<(unsigned)b, T, 0, s>>>(a);
+}
+
+template <int D, bool CL>
+cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
+{
+    static_assert(kNumSearchShapes == 6, "one case per shape");
+    switch (shape) {
+    case 0: launch_shape<D, CL, 0>(a, sms, s); break;
+    case 1: launch_shape<D, CL, 1>(a, sms, s); break;
+    case 2: launch_shape<D, CL, 2>(a, sms, s); break;
+    case 3: launch_shape<D, CL, 3>(a, sms, s); break;
+    case 4: launch_shape<D, CL, 4>(a, sms, s); break;
+    case 5: launch_shape<D, CL, 5>(a, sms, s); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+}  // namespace emst

@@ -1,0 +1,11 @@
+// cnns_t2.cu -- the component search kernel for 2D points, every launch shape.
+#include "cnns_search.cuh"
+
+namespace emst {
+
+cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s)
+{
+    return clouds ? launch_dim<2, true>(a, shape, sms, s) : launch_dim<2, false>(a, shape, sms, s);
+}
+
+}  // namespace emst

@@ -1,0 +1,11 @@
+// cnns_t3.cu -- the component search kernel for 3D points, every launch shape.
+#include "cnns_search.cuh"
+
+namespace emst {
+
+cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s)
+{
+    return clouds ? launch_dim<3, true>(a, shape, sms, s) : launch_dim<3, false>(a, shape, sms, s);
+}
+
+}  // namespace emst

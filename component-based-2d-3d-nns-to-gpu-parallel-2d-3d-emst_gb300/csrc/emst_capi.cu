@@ -304,6 +304,7 @@ emst_status build_graph(emst_ctx* x)
     std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
                                     c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
                                     c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p, c.dflag.p, c.sel_tmp.p,
+                                    (const void*)(intptr_t)emst::search_shape_of(c),
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
@@ -405,8 +406,10 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         c.search_mode = (cfg->search_mode == 1 || c.keep_table) ? 1 : 0;
         c.cnns_warp = cfg->search_mode == 2;
         c.use_graph = cfg->host_rounds == 0;
+        if (cfg->search_shape > 0) c.search_shape = cfg->search_shape - 1;
     }
     cudaError_t e = cudaSetDevice(c.device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = emst::ensure(c.ctr, 1);
     if (e == cudaSuccess) e = emst::ensure(c.dlen, 1);
@@ -796,6 +799,70 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
         EMST_CUDA(x, cudaMemcpyAsync(lengths, c.dlen.p, sizeof(double) * n_clouds, cudaMemcpyDeviceToHost, s),
                   "download");
     return read_counters(x);
+}
+
+emst_status emst_search_shape_info(int* count, int* threads, int* min_blocks, int cap)
+{
+    if (count) *count = emst::kNumSearchShapes;
+    for (int k = 0; k < emst::kNumSearchShapes && k < cap; ++k) {
+        if (threads) threads[k] = emst::kSearchShapes[k].threads;
+        if (min_blocks) min_blocks[k] = emst::kSearchShapes[k].min_blocks;
+    }
+    return EMST_OK;
+}
+
+emst_status emst_get_search_shape(emst_ctx* x, int* search_shape)
+{
+    if (!x || !search_shape) return EMST_EINVAL;
+    *search_shape = x->c.search_shape >= 0 ? x->c.search_shape + 1 : 0;
+    return EMST_OK;
+}
+
+emst_status emst_autotune(emst_ctx* x, const float* points, int64_t n, int dim, int* best, double* ms, int cap)
+{
+    if (!x) return EMST_EINVAL;
+    Ctx& c = x->c;
+    if (c.search_mode != 0 || c.cnns_warp)
+        return set_err(x, EMST_EINVAL, "the autotuner tunes the component search (search_mode 0)");
+    if (!points || n < 2) return set_err(x, EMST_EINVAL, "the autotuner needs at least two host points");
+    EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    EMST_CUDA(x, cudaEventCreate(&e0), "event");
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_err(x, EMST_ECUDA, "event");
+    }
+    emst_status st = EMST_OK;
+    double best_ms = 1e300;
+    int best_k = 0;
+    for (int k = 0; k < emst::kNumSearchShapes && st == EMST_OK; ++k) {
+        c.search_shape = k;
+        double t = 1e300;
+        for (int rep = 0; rep < 3 && st == EMST_OK; ++rep) {  // rep 0 warms up (and builds the graph)
+            if ((st = do_initialize(x, points, n, dim, 0)) != EMST_OK) break;
+            cudaEventRecord(e0, c.stream);
+            if ((st = do_run(x)) != EMST_OK) break;
+            cudaEventRecord(e1, c.stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                st = set_err(x, EMST_ECUDA, "autotune timing");
+                break;
+            }
+            float el = 0.f;
+            cudaEventElapsedTime(&el, e0, e1);
+            if (rep > 0 && el < t) t = el;
+        }
+        if (ms && k < cap) ms[k] = t;
+        if (t < best_ms) {
+            best_ms = t;
+            best_k = k;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != EMST_OK) return st;
+    c.search_shape = best_k;
+    if (best) *best = best_k + 1;
+    return EMST_OK;
 }
 
 emst_status emst_solve_device(emst_ctx* x, const float* d_points, int64_t n, int dim, int32_t* d_uv,

@@ -118,6 +118,8 @@ struct Ctx {
     int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu)
     bool cnns_warp = false;   // component search: warp per 32 queries instead of thread per query
     bool use_graph = true;    // component search: run the round loop as one CUDA graph
+    int search_shape = -1;    // component search launch shape (kSearchShapes); -1: default for the dimension
+    int sms = 152;            // multiprocessors of the device
     DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
     DevBuf<unsigned char> dflag, sel_tmp;  // per point: dirty flag; compaction scratch
@@ -170,6 +172,52 @@ cudaError_t cnns_init(Ctx& c);
 cudaError_t cnns_node_labels(Ctx& c);
 cudaError_t cnns_select(Ctx& c);
 cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out);
+
+// Arguments of one component-search launch (cnns_search.cuh).
+struct CnnsArgs {
+    const float4* spl;
+    const uint32_t* perm;
+    const float4* nlo;
+    const float4* nhi;
+    const uint32_t* nlab;
+    uint32_t n, L;
+    const uint32_t* list;
+    const uint32_t* n_list;
+    const uint32_t* lab;
+    uint64_t* ckey;
+    uint32_t* selq;
+    uint64_t* selkey;
+    uint32_t* prov;
+    uint32_t* n_prov;
+    float* lbp;
+    const uint32_t* clb;
+    int pass;
+    unsigned char* dflag;
+    const uint32_t* pcloud;
+    const uint32_t* ncloud;
+    unsigned long long* stats;
+};
+
+// Launch shapes of the component search: threads per block and the minimum
+// number of resident blocks per SM the compiler must fit (which caps the
+// registers per thread).  emst_autotune times them; the defaults per
+// dimension are the fastest measured on GB300.
+struct SearchShape {
+    int threads, min_blocks;
+};
+constexpr int kNumSearchShapes = 6;
+constexpr SearchShape kSearchShapes[kNumSearchShapes] = {{256, 4}, {256, 5}, {256, 6}, {128, 8}, {128, 12}, {512, 3}};
+
+// Shape used by a context: its own choice, else the default for the dimension.
+constexpr int kDefaultShape2 = 1, kDefaultShape3 = 1;
+inline int search_shape_of(const Ctx& c)
+{
+    if (c.search_shape >= 0 && c.search_shape < kNumSearchShapes) return c.search_shape;
+    return c.dim == 2 ? kDefaultShape2 : kDefaultShape3;
+}
+
+cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
+cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
 
 template <typename T>
 cudaError_t ensure(DevBuf<T>& b, size_t n)

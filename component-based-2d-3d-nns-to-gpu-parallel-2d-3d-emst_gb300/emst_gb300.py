@@ -32,7 +32,7 @@ class EmstError(RuntimeError):
 class Config(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_rounds", ctypes.c_int), ("warps_per_block", ctypes.c_int),
                 ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("search_mode", ctypes.c_int),
-                ("host_rounds", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("host_rounds", ctypes.c_int), ("search_shape", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class Profile(ctypes.Structure):
@@ -75,6 +75,8 @@ def lib():
             "emst_get_rescaled": [P, P, P, i64], "emst_solve": [P, P, i64, I, P, P, P],
             "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
             "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
+            "emst_search_shape_info": [P, P, P, I], "emst_autotune": [P, P, i64, I, P, P, I],
+            "emst_get_search_shape": [P, P],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -86,6 +88,16 @@ def lib():
     return _lib
 
 
+def search_shapes():
+    """Launch shapes of the component search: (count, threads per block, min blocks per SM)."""
+    cnt = ctypes.c_int()
+    lib().emst_search_shape_info(ctypes.byref(cnt), None, None, 0)
+    t = np.zeros(cnt.value, np.int32)
+    m = np.zeros(cnt.value, np.int32)
+    lib().emst_search_shape_info(ctypes.byref(cnt), _p(t), _p(m), cnt.value)
+    return cnt.value, t, m
+
+
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
@@ -94,9 +106,9 @@ class Emst:
     """One context = one CUDA stream on one device."""
 
     def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False,
-                 search_mode=0, host_rounds=False):
+                 search_mode=0, host_rounds=False, search_shape=0):
         cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0,
-                     int(search_mode), 1 if host_rounds else 0)
+                     int(search_mode), 1 if host_rounds else 0, int(search_shape))
         h = ctypes.c_void_p()
         st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:
@@ -247,6 +259,21 @@ class Emst:
                                          ctypes.byref(ne)))
         eo = np.concatenate([[0], np.cumsum(np.maximum(sizes - 1, 0))])
         return [uv[eo[i]:eo[i + 1]].copy() for i in range(len(clouds))], lens
+
+    def autotune(self, pts):
+        """Times every launch shape on pts; keeps the fastest. -> (search_shape, ms per shape)."""
+        pts = np.ascontiguousarray(pts, np.float32)
+        cnt, _, _ = search_shapes()
+        ms = np.zeros(cnt, np.float64)
+        best = ctypes.c_int()
+        self._chk(lib().emst_autotune(self.h, _p(pts), len(pts), pts.shape[1], ctypes.byref(best), _p(ms), cnt))
+        self.n, self.dim = len(pts), pts.shape[1]
+        return best.value, ms
+
+    def search_shape(self):
+        v = ctypes.c_int()
+        self._chk(lib().emst_get_search_shape(self.h, ctypes.byref(v)))
+        return v.value
 
     def solve_device(self, d_points, n, dim, d_uv, d_length):
         ne = ctypes.c_int64()

@@ -55,7 +55,10 @@ typedef struct {
                               2: component search, one warp per 32 queries */
     int host_rounds;       /* != 0: drive the component search's rounds from
                               the host instead of one CUDA graph */
-    int reserved[5];
+    int search_shape;      /* component search launch shape: 0 = default for
+                              the dimension, k = entry k-1 of the shape table
+                              (emst_search_shape_info); see emst_autotune */
+    int reserved[4];
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel
@@ -202,6 +205,24 @@ emst_status emst_solve_batch(emst_ctx* ctx, const float* points, const int64_t* 
  * termination read. */
 emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
                               double* d_length, int64_t* n_edges);
+
+/* ---------------------------------------------------------------------------
+ * Launch-shape autotuner (no counterpart in the reference, whose kernels use
+ * fixed 4x4x4 / 8x8 thread blocks: EMSTOperators.h:1405-1416)
+ * ------------------------------------------------------------------------- */
+
+/* The component search's launch shapes: *count entries; per entry k
+ * (emst_config.search_shape = k + 1) the threads per block and the minimum
+ * resident blocks per SM it is compiled for (cap entries written). */
+emst_status emst_search_shape_info(int* count, int* threads, int* min_blocks, int cap);
+
+/* Solves `points` (host, n x dim) once per launch shape after a warm-up
+ * solve, keeps the fastest shape for this context and returns its
+ * emst_config.search_shape value in *best.  ms (optional, cap entries): the
+ * best of two timed solves per shape.  Afterwards the context holds a
+ * finished solve of `points`.  Component search mode only. */
+emst_status emst_autotune(emst_ctx* ctx, const float* points, int64_t n, int dim, int* best, double* ms, int cap);
+emst_status emst_get_search_shape(emst_ctx* ctx, int* search_shape);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free region table

@@ -223,6 +223,51 @@ def test_batch_workload_512_clouds_vs_oracle(gpu_lib):
             assert np.array_equal(_canon(uvs[i]), _canon(ref_uv))
 
 
+@pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 20000), ("uniform", 2, 20000), ("dups", 3, 3000)])
+def test_every_search_shape_same_edges(gpu_lib, kind, dim, n):
+    """Every launch shape of the component search gives the same edge set,
+    single clouds and batches alike."""
+    pts = family(kind, n, dim, 41)
+    with gpu_lib.Emst() as e:
+        ref, ref_len = e.solve(pts)
+    count, threads, min_blocks = gpu_lib.search_shapes()
+    assert count >= 2 and all(t % 32 == 0 for t in threads) and all(m >= 1 for m in min_blocks)
+    for k in range(1, count + 1):
+        with gpu_lib.Emst(search_shape=k) as e:
+            assert e.search_shape() == k
+            uv, ln = e.solve(pts)
+            assert np.array_equal(_canon(uv), _canon(ref)), k
+            assert ln == pytest.approx(ref_len, rel=1e-12)
+            uvs, _ = e.solve_batch([pts, pts[: n // 3]])
+            assert np.array_equal(_canon(uvs[0]), _canon(ref)), k
+
+
+def test_autotune_picks_a_shape_and_keeps_edges(gpu_lib):
+    """emst_autotune times every shape, keeps the fastest, and later solves
+    with it give the default shape's edge set."""
+    pts = family("cluster", 30000, 3, 42)
+    with gpu_lib.Emst() as e:
+        ref, _ = e.solve(pts)
+        assert e.search_shape() == 0
+        best, ms = e.autotune(pts)
+        count, _, _ = gpu_lib.search_shapes()
+        assert 1 <= best <= count and e.search_shape() == best
+        assert np.all(np.isfinite(ms)) and np.all(ms > 0) and ms[best - 1] == ms.min()
+        uv, _ = e.solve(pts)
+        assert np.array_equal(_canon(uv), _canon(ref))
+        other = family("uniform", 5000, 2, 43)
+        uv2, _ = e.solve(other)
+    with gpu_lib.Emst() as e:
+        ref2, _ = e.solve(other)
+    assert np.array_equal(_canon(uv2), _canon(ref2))
+
+
+def test_autotune_rejects_static_mode(gpu_lib):
+    with gpu_lib.Emst(search_mode=1) as e:
+        with pytest.raises(gpu_lib.EmstError):
+            e.autotune(family("uniform", 1000, 2, 44))
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
