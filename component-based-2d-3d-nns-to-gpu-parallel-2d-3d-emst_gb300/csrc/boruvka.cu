@@ -27,6 +27,7 @@ namespace emst {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr uint32_t kNoPartner = 0xffffffffu;  // selq of a point without a certified partner
 
 // Warp-aggregated append of `val` to list[] through counter *cnt.
 __device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* list, uint32_t* cnt)
@@ -113,8 +114,11 @@ __global__ void k_resolve(const uint32_t* __restrict__ prov, const uint32_t* __r
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const uint32_t p = prov[i];
         const uint32_t lp = lab[p];
-        if (selkey[p] != ckey[lp]) continue;
-        const uint32_t mx = max(perm[p], perm[selq[p]]);
+        const uint32_t q = selq[p];
+        // a result without a partner (not certified) cannot be the winner; if
+        // it held the component's key the hook reports it (no winner found)
+        if (selkey[p] != ckey[lp] || q == kNoPartner) continue;
+        const uint32_t mx = max(perm[p], perm[q]);
         atomicMin((unsigned long long*)&cmax[lp], (unsigned long long)(((uint64_t)mx << 32) | p));
     }
 }

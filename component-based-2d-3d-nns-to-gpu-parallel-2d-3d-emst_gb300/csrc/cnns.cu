@@ -414,12 +414,18 @@ cudaError_t cnns_select(Ctx& c)
                     c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2,
                     st);
         } else {
-            CnnsArgs a{c.spl.p, c.perm.p, c.nlo.p,  c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
-                       cnt,     c.lab.p,  c.ckey.p, c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p,
-                       c.clb.p, pass,     c.dflag.p, pc,     nc,        st};
+            CnnsArgs a{c.spl.p,  c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
+                       cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
+                       c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
+                       &d->round};
             const int shape = search_shape_of(c);
-            cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, shape, c.sms, c.stream)
-                                        : launch_cnns_t3(a, pc != nullptr, shape, c.sms, c.stream);
+            const bool learned = c.learned && pass == 1 && !pc;
+            if (pass == 1 && c.trace_cap > 0 && !learned) {
+                cudaError_t et = proposal_trace_begin(c);
+                if (et != cudaSuccess) return et;
+            }
+            cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
+                                        : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
             if (pass == 1) {
                 size_t tbytes = c.sel_tmp.cap;
@@ -431,6 +437,10 @@ cudaError_t cnns_select(Ctx& c)
         c.nns_launches++;
     }
     c.launches += 3;
+    if (c.trace_cap > 0 && !(c.learned && !pc)) {
+        cudaError_t et = proposal_trace_end(c);
+        if (et != cudaSuccess) return et;
+    }
     return cudaGetLastError();
 }
 

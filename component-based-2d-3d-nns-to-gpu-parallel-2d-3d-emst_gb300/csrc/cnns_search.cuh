@@ -6,6 +6,7 @@
 
 #include "emst_ctx.h"
 #include "emst_device.cuh"
+#include "proposal.cuh"
 
 namespace emst {
 
@@ -37,8 +38,9 @@ __device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* l
 // CL: batched clouds (pcloud / ncloud given); a candidate must share the
 // query's cloud.
 // TPB threads per block, at least MINB blocks resident per SM (the launch
-// shape; kSearchShapes lists the instantiated pairs).
-template <int D, bool CL, int TPB, int MINB>
+// shape; kSearchShapes lists the instantiated pairs).  LEARN: first pass
+// under the learned proposal (proposal.cuh) instead of the fixed rule.
+template <int D, bool CL, int TPB, int MINB, bool LEARN = false>
 __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 {
     const float4* __restrict__ spl = a.spl;
@@ -63,6 +65,21 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     const uint32_t* __restrict__ ncloud = a.ncloud;
     unsigned long long* __restrict__ stats = a.stats;
     constexpr int kTStack = 48;
+    constexpr int kWarps = TPB / 32;
+    __shared__ __align__(16) unsigned char s_prop[LEARN ? sizeof(prop::Frag) + kWarps * (512 + 256) : 16];
+    prop::Frag& W = *reinterpret_cast<prop::Frag*>(s_prop);
+    __nv_bfloat16* s_stage = nullptr;
+    float* s_outs = nullptr;
+    int round = 0;
+    if constexpr (LEARN) {
+        s_stage = reinterpret_cast<__nv_bfloat16*>(s_prop + sizeof(prop::Frag)) + (threadIdx.x >> 5) * 256;
+        s_outs = reinterpret_cast<float*>(s_prop + sizeof(prop::Frag) + kWarps * 512) + (threadIdx.x >> 5) * 64;
+        const uint4* src = reinterpret_cast<const uint4*>(a.frag);
+        uint4* dst = reinterpret_cast<uint4*>(s_prop);
+        for (int i = threadIdx.x; i < (int)(sizeof(prop::Frag) / 16); i += TPB) dst[i] = src[i];
+        round = *a.round;
+        __syncthreads();
+    }
     const uint32_t total = *n_list;
     for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
         const uint32_t qi = base0 + threadIdx.x;
@@ -72,18 +89,40 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
         const float lb0 = listed ? lbp[me] : 0.f;
         bool valid = listed, deferred = false;
         float cb = INFINITY;
+        float cap = INFINITY;  // first-pass search radius (learned proposal)
         if (listed) {
             const uint64_t k = __ldcg(&ckey[labp]);
             cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
-            if (lb0 > cb) {
-                valid = false;  // cannot hold its component's minimum this round
-            } else if (pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
-                valid = false;  // not among its component's most promising points: second pass
-                deferred = true;
-            }
+            if (lb0 > cb) valid = false;  // cannot hold its component's minimum this round
         }
-        // second-pass flags, compacted in leaf order after the first pass
-        if (listed && pass == 1) dflag[me] = deferred ? 1 : 0;
+        if constexpr (LEARN) {
+            // the whole warp is converged here: one tensor-core inference for
+            // its 32 queries, features in registers
+            float f[prop::kIn];
+            if (listed) {
+                const uint32_t ol = L + (me >> 5);
+                const float4 lo = __ldg(&nlo[ol]), hi = __ldg(&nhi[ol]);
+                const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = D == 3 ? hi.z - lo.z : 0.f;
+                prop::features(lb0, __uint_as_float(__ldcg(&clb[labp])), cb, ex * ex + ey * ey + ez * ez,
+                               __ldg(&nlab[ol]) == labp, round, f);
+            } else {
+#pragma unroll
+                for (int i = 0; i < prop::kIn; ++i) f[i] = 0.f;
+            }
+            float o0, o1;
+            prop::infer_warp(W, f, s_stage, s_outs, o0, o1);
+            if (valid) {
+                cap = exp2f(fminf(8.f * o0 + a.margin, 126.f));
+                if (o1 < 0.f || cap < lb0) {
+                    valid = false;  // predicted not to hold the minimum: second pass
+                    deferred = true;
+                }
+            }
+        } else if (valid && pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
+            valid = false;  // not among its component's most promising points: second pass
+            deferred = true;
+        }
+        bool again = false;  // first-pass search cut short by the proposal's radius
 
         bool record = false;
         uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
@@ -92,6 +131,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
             const int op = (int)perm[me];
             const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;  // the query's cloud (batches)
             float bd = INFINITY, cut = INFINITY;
+            bool capped = false;  // a node was left out only by the radius
             int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
             int bs = -1;  // leaf position of the best
 
@@ -166,8 +206,11 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 ++st_nodes;
                 const float ls = node_lb(sib);
                 if (!(ls < INFINITY)) continue;
-                if (ls > fminf(bd, cb)) {
-                    if (ls <= bd) cut = fminf(cut, ls);
+                if (ls > fminf(fminf(bd, cb), cap)) {
+                    if (ls <= bd) {
+                        cut = fminf(cut, ls);
+                        if (LEARN && ls <= cb) capped = true;
+                    }
                     continue;
                 }
                 int top = 0;
@@ -185,8 +228,9 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                             // bound re-checked: bd may have shrunk since the push
                             const float lb = node_lb(node);
                             if (!(lb < INFINITY) || lb > bd) continue;
-                            if (lb > cb) {
+                            if (lb > fminf(cb, cap)) {
                                 cut = fminf(cut, lb);
+                                if (LEARN && lb <= cb) capped = true;
                                 continue;
                             }
                             leaf = node - L;
@@ -194,7 +238,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                         }
                         const uint32_t c0 = 2 * node, c1 = c0 + 1;
                         const float l0 = node_lb(c0), l1 = node_lb(c1);
-                        const float lim = fminf(bd, cb);
+                        const float lim = fminf(fminf(bd, cb), cap);
                         // push the farther child first so the nearer one is searched next
                         const bool near0 = l0 <= l1;
                         const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
@@ -204,9 +248,15 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                             break;
                         }
                         if (lf < INFINITY && lf <= lim) stack[top++] = cf;
-                        else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
+                        else if (lf <= bd && lf < INFINITY) {
+                            cut = fminf(cut, lf);
+                            if (LEARN && lf <= cb) capped = true;
+                        }
                         if (ln < INFINITY && ln <= lim) stack[top++] = cn;
-                        else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
+                        else if (ln <= bd && ln < INFINITY) {
+                            cut = fminf(cut, ln);
+                            if (LEARN && ln <= cb) capped = true;
+                        }
                     }
                     if (leaf != kNone) {
                         scan_leaf(leaf);
@@ -216,6 +266,9 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 }
             }
             const bool exact = bs >= 0 && bd < cut;
+            // nodes left out only by the radius may hold a closer point: search
+            // again in the second pass (the lower bound below stays valid)
+            again = capped && !exact;
             lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
             if (bs >= 0) {
                 if (bo < 0) bo = (int)__ldg(&perm[bs]);
@@ -235,21 +288,29 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
         // lanes of a diverged warp drift into different iterations and the
         // next traversals run with a fraction of the warp active.
         __syncwarp();
+        // second-pass flags, compacted in leaf order after the first pass
+        if (listed && pass == 1) dflag[me] = (deferred || again) ? 1 : 0;
         warp_append(record, me, prov, n_prov);
         if (stats) {
-            unsigned long long a = st_leaves, b = st_nodes, c = st_cands, q = valid ? 1ull : 0ull;
+            unsigned long long sl = st_leaves, sn = st_nodes, sc = st_cands, q = valid ? 1ull : 0ull;
             for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_xor_sync(kFull, a, o);
-                b += __shfl_xor_sync(kFull, b, o);
-                c += __shfl_xor_sync(kFull, c, o);
+                sl += __shfl_xor_sync(kFull, sl, o);
+                sn += __shfl_xor_sync(kFull, sn, o);
+                sc += __shfl_xor_sync(kFull, sc, o);
                 q += __shfl_xor_sync(kFull, q, o);
             }
+            const unsigned first = __ballot_sync(kFull, valid && pass == 1);
+            const unsigned resumed = __ballot_sync(kFull, again);
+            const unsigned later = __ballot_sync(kFull, deferred);
             if ((threadIdx.x & 31) == 0) {
-                atomicAdd(&stats[0], a);
-                atomicAdd(&stats[1], b);
-                atomicAdd(&stats[2], c);
+                atomicAdd(&stats[0], sl);
+                atomicAdd(&stats[1], sn);
+                atomicAdd(&stats[2], sc);
                 atomicAdd(&stats[3], 1ull);
                 atomicAdd(&stats[4], q);
+                atomicAdd(&stats[5], (unsigned long long)__popc(first));
+                atomicAdd(&stats[6], (unsigned long long)__popc(resumed));
+                atomicAdd(&stats[7], (unsigned long long)__popc(later));
             }
         }
     }
@@ -258,7 +319,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 
 // Launch of one shape; the grid covers the list's upper bound `a.n` with at
 // most four waves of resident blocks (the kernel strides over the rest).
-template <int D, bool CL, int I>
+template <int D, bool CL, int I, bool LEARN>
 void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 {
     constexpr int T = kSearchShapes[I].threads, M = kSearchShapes[I].min_blocks;
@@ -266,20 +327,20 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
     const uint64_t cap = (uint64_t)sms * M * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_cnns_t<D, CL, T, M><<<(unsigned)b, T, 0, s>>>(a);
+    k_cnns_t<D, CL, T, M, LEARN><<<(unsigned)b, T, 0, s>>>(a);
 }
 
-template <int D, bool CL>
+template <int D, bool CL, bool LEARN = false>
 cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
 {
     static_assert(kNumSearchShapes == 6, "one case per shape");
     switch (shape) {
-    case 0: launch_shape<D, CL, 0>(a, sms, s); break;
-    case 1: launch_shape<D, CL, 1>(a, sms, s); break;
-    case 2: launch_shape<D, CL, 2>(a, sms, s); break;
-    case 3: launch_shape<D, CL, 3>(a, sms, s); break;
-    case 4: launch_shape<D, CL, 4>(a, sms, s); break;
-    case 5: launch_shape<D, CL, 5>(a, sms, s); break;
+    case 0: launch_shape<D, CL, 0, LEARN>(a, sms, s); break;
+    case 1: launch_shape<D, CL, 1, LEARN>(a, sms, s); break;
+    case 2: launch_shape<D, CL, 2, LEARN>(a, sms, s); break;
+    case 3: launch_shape<D, CL, 3, LEARN>(a, sms, s); break;
+    case 4: launch_shape<D, CL, 4, LEARN>(a, sms, s); break;
+    case 5: launch_shape<D, CL, 5, LEARN>(a, sms, s); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

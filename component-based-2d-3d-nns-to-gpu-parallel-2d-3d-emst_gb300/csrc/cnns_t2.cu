@@ -3,8 +3,9 @@
 
 namespace emst {
 
-cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s)
+cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s)
 {
+    if (learned) return launch_dim<2, false, true>(a, shape, sms, s);  // single clouds only
     return clouds ? launch_dim<2, true>(a, shape, sms, s) : launch_dim<2, false>(a, shape, sms, s);
 }
 

@@ -5,6 +5,8 @@
 // test, iteration++, find-min-1 (computeOctants + findNextClosestPoint),
 // find-min-2 (component min pair), connect-and-union; the loop stops when one
 // component remains or at the 100-round cap (:210).
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -13,12 +15,14 @@
 
 #include "../../include/emst.h"
 #include "emst_ctx.h"
+#include "proposal.cuh"
 
 struct emst_ctx {
     emst::Ctx c;
     int stage = 0;  // 0: needs flatten, 1: flattened, 2: octants, 3: next-closest, 4: min-pair
     int64_t last_edges = 0;
     emst::DevBuf<int32_t> tmp_i32;
+    emst::DevBuf<float> tmp_f32;
     // phase timing: (phase, start, end) event pairs recorded since the last sync
     struct Pending {
         int phase;
@@ -250,8 +254,8 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     c.launches = 0;
     c.nns_launches = 0;
     if (c.profile) {
-        EMST_CUDA(x, emst::ensure(c.nstats, 5), "alloc");
-        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 5 * sizeof(unsigned long long), c.stream), "stats");
+        EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), c.stream), "stats");
     }
     for (double& v : x->ms) v = 0.0;
     {
@@ -304,7 +308,9 @@ emst_status build_graph(emst_ctx* x)
     std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
                                     c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
                                     c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p, c.dflag.p, c.sel_tmp.p,
-                                    (const void*)(intptr_t)emst::search_shape_of(c),
+                                    (const void*)(intptr_t)emst::search_shape_of(c), c.pfrag.p,
+                                    (const void*)(intptr_t)(c.learned ? 1 : 0), c.trace.p,
+                                    (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
@@ -449,6 +455,9 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.dirty);
     emst::release(c.dirty2);
     emst::release(c.dflag);
+    emst::release(c.pfrag);
+    emst::release(c.trace);
+    emst::release(c.trace_ctl);
     emst::release(c.sel_tmp);
     emst::release(c.lbp);
     emst::release(c.clb);
@@ -488,6 +497,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.lpart);
     emst::release(c.dlen);
     emst::release(x->tmp_i32);
+    emst::release(x->tmp_f32);
     for (auto& p : x->pending) x->pool.push_back({p.a, p.b});
     for (auto& p : x->pool) {
         cudaEventDestroy(p.first);
@@ -664,8 +674,11 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     out->octant_launches = x->c.nns_launches;
     out->rounds = x->c.round;
     if (x->c.profile && x->c.nstats.p) {
-        unsigned long long st[5];
+        unsigned long long st[8];
         EMST_CUDA(x, cudaMemcpy(st, x->c.nstats.p, sizeof(st), cudaMemcpyDeviceToHost), "stats");
+        out->first_pass_searches = (int64_t)st[5];
+        out->first_pass_resumed = (int64_t)st[6];
+        out->first_pass_deferred = (int64_t)st[7];
         out->leaf_visits = (int64_t)st[0];
         out->node_tests = (int64_t)st[1];
         out->candidates = (int64_t)st[2];
@@ -768,8 +781,8 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
     c.nns_launches = 0;
     for (double& v : x->ms) v = 0.0;
     if (c.profile) {
-        EMST_CUDA(x, emst::ensure(c.nstats, 5), "alloc");
-        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 5 * sizeof(unsigned long long), s), "stats");
+        EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), s), "stats");
     }
     {
         Timed t(x, PH_GRID);
@@ -799,6 +812,71 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
         EMST_CUDA(x, cudaMemcpyAsync(lengths, c.dlen.p, sizeof(double) * n_clouds, cudaMemcpyDeviceToHost, s),
                   "download");
     return read_counters(x);
+}
+
+emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin)
+{
+    if (!x) return EMST_EINVAL;
+    Ctx& c = x->c;
+    if (!weights) {
+        c.learned = false;
+        return EMST_OK;
+    }
+    if (c.search_mode != 0 || c.cnns_warp)
+        return set_err(x, EMST_EINVAL, "the learned proposal drives the component search (search_mode 0)");
+    if (!(margin >= 0.f && margin <= 64.f)) return set_err(x, EMST_EINVAL, "margin must be in [0, 64]");
+    for (int i = 0; i < emst::prop::kNumWeights; ++i)
+        if (!std::isfinite(weights[i])) return set_err(x, EMST_EINVAL, "non-finite proposal weight");
+    EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
+    EMST_CUDA(x, emst::ensure(c.pfrag, emst::proposal_frag_bytes()), "alloc");
+    EMST_CUDA(x, emst::ensure(x->tmp_f32, (size_t)emst::prop::kNumWeights), "alloc");
+    EMST_CUDA(x, cudaMemcpyAsync(x->tmp_f32.p, weights, sizeof(float) * emst::prop::kNumWeights,
+                                 cudaMemcpyHostToDevice, c.stream), "upload");
+    EMST_CUDA(x, emst::proposal_pack(x->tmp_f32.p, c.pfrag.p, c.stream), "pack");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+    c.learned = true;
+    c.margin = margin;
+    return EMST_OK;
+}
+
+emst_status emst_trace_enable(emst_ctx* x, int64_t capacity, int sample_shift)
+{
+    if (!x || capacity < 0 || capacity > 0xfffffff0ll || sample_shift < 0 || sample_shift > 24) return EMST_EINVAL;
+    Ctx& c = x->c;
+    if (capacity > 0 && (c.search_mode != 0 || c.cnns_warp))
+        return set_err(x, EMST_EINVAL, "traces come from the component search (search_mode 0)");
+    EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
+    c.trace_cap = capacity;
+    c.trace_shift = sample_shift;
+    if (capacity == 0) return EMST_OK;
+    EMST_CUDA(x, emst::ensure(c.trace, (size_t)capacity * emst::prop::kRec), "alloc trace");
+    EMST_CUDA(x, emst::ensure(c.trace_ctl, 2), "alloc");
+    EMST_CUDA(x, cudaMemsetAsync(c.trace_ctl.p, 0, 2 * sizeof(uint32_t), c.stream), "trace reset");
+    return EMST_OK;
+}
+
+emst_status emst_get_trace(emst_ctx* x, float* records, int64_t cap, int64_t* count)
+{
+    if (!x || !count) return EMST_EINVAL;
+    Ctx& c = x->c;
+    *count = 0;
+    if (c.trace_cap == 0) return EMST_OK;
+    uint32_t ctl[2] = {0, 0};
+    EMST_CUDA(x, cudaMemcpyAsync(ctl, c.trace_ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost, c.stream), "trace count");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+    const int64_t have = std::min<int64_t>((int64_t)ctl[0], c.trace_cap);
+    *count = have;
+    if (records && cap > 0 && have > 0)
+        EMST_CUDA(x, cudaMemcpy(records, c.trace.p, sizeof(float) * emst::prop::kRec * std::min(have, cap),
+                                cudaMemcpyDeviceToHost), "trace download");
+    return EMST_OK;
+}
+
+emst_status emst_get_trace_device(emst_ctx* x, const float** d_records, int64_t* count)
+{
+    if (!x || !d_records) return EMST_EINVAL;
+    *d_records = x->c.trace.p;
+    return emst_get_trace(x, nullptr, 0, count);
 }
 
 emst_status emst_search_shape_info(int* count, int* threads, int* min_blocks, int cap)

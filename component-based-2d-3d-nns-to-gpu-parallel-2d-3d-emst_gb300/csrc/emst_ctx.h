@@ -136,7 +136,18 @@ struct Ctx {
     DevBuf<uint32_t> ncloud;             // per node: (first cloud << 16) | last cloud of its points
     DevBuf<uint32_t> bcursor, bedges;            // output scatter cursors, edges with global ids
     DevBuf<uint32_t> clb;            // per root: min lbp over its dirty points (float bits)
-    DevBuf<unsigned long long> nstats;  // region search: leaf visits, node tests, candidates, warps
+    DevBuf<unsigned long long> nstats;  // search counters (emst_profile), 8 entries
+
+    // learned proposal (proposal.cuh): packed weights, radius margin (log2)
+    bool learned = false;
+    float margin = 1.f;
+    DevBuf<unsigned char> pfrag;
+    // search traces for training: records of prop::kRec floats, 1 in 2^shift
+    // first-pass queries; ctl = {records written, first record of the round}
+    DevBuf<float> trace;
+    int64_t trace_cap = 0;
+    int trace_shift = 0;
+    DevBuf<uint32_t> trace_ctl;
 
     int round = 0;        // rounds started
     int phase = 0;        // 0 = not initialised, 1 = initialised
@@ -196,6 +207,9 @@ struct CnnsArgs {
     const uint32_t* pcloud;
     const uint32_t* ncloud;
     unsigned long long* stats;
+    const void* frag;  // learned proposal: fragment-ordered weights (prop::Frag), or null
+    float margin;      // learned proposal: log2 margin added to the predicted radius
+    const int* round;  // rounds started (device)
 };
 
 // Launch shapes of the component search: threads per block and the minimum
@@ -216,8 +230,14 @@ inline int search_shape_of(const Ctx& c)
     return c.dim == 2 ? kDefaultShape2 : kDefaultShape3;
 }
 
-cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
-cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
+cudaError_t proposal_pack(const float* d_weights, void* d_frag, cudaStream_t s);
+size_t proposal_frag_bytes();
+cudaError_t proposal_trace_begin(Ctx& c);
+cudaError_t proposal_trace_end(Ctx& c);
+uint64_t splitmix(uint64_t& s);
+
+cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
+cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 
 template <typename T>
 cudaError_t ensure(DevBuf<T>& b, size_t n)

@@ -1,0 +1,152 @@
+// proposal.cuh -- the learned search proposal: features, the 8-32-32-2 MLP on
+// BF16 tensor-core MMA (m16n8k16, FP32 accumulate), and the weight layouts
+// shared by the fused inference (cnns_search.cuh) and the training kernels
+// (proposal.cu).
+//
+// The proposal replaces the fixed first-pass rule of the component search
+// ("search now when lbp <= 4 x the component's smallest lbp, else defer").
+// For each dirty point it predicts
+//   out0: log2(d2 of its component's shortest outgoing edge) / 8 -- the
+//         search radius: the first-pass search stops at that radius;
+//   out1: logit of "this point can hold the component's minimum" -- the
+//         visit order: points below 0 wait for the second pass.
+// Neither output changes what is found.  A first-pass search cut short by
+// the radius leaves a certified lower bound and goes to the second pass,
+// which searches with the component's real bound, so every component's
+// minimum -- and the edge set -- is the plain method's.
+#pragma once
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+namespace emst {
+
+namespace prop {
+
+constexpr int kIn = 8, kHid = 32, kOut = 2;
+// FP32 master weights, row-major [in][out]: W1 b1 W2 b2 W3 b3.
+constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kIn * kHid, kOffW2 = kOffB1 + kHid, kOffB2 = kOffW2 + kHid * kHid,
+              kOffW3 = kOffB2 + kHid, kOffB3 = kOffW3 + kHid * kOut, kNumWeights = kOffB3 + kOut;  // 1410
+// Trace record: 8 features, regression target, class label, regression mask, spare.
+constexpr int kRec = 12;
+
+// Fragment-ordered BF16 weights for the fused inference, one 32-bit register
+// pair per lane and MMA: layer 1 (k 8 of 16 used: only register 0 of B is
+// non-zero) 4 n-tiles; layer 2 4 n-tiles x 2 k-tiles; layer 3 1 n-tile x 2
+// k-tiles; then the FP32 biases.
+struct Frag {
+    uint32_t w1[4][32];        // [ntile][lane]: B register 0 (rows 2t, 2t+1 of W1)
+    uint2 w2[4][2][32];        // [ntile][ktile][lane]
+    uint2 w3[2][32];           // [ktile][lane]
+    float b1[kHid], b2[kHid], b3[8];
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (low half)
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// D = A(16x16, row) * B(16x8, col) + D, BF16 inputs, FP32 accumulate.
+__device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float lg8(float d2) { return log2f(fmaxf(d2, 1e-12f)) * 0.125f; }
+
+// Features of one dirty point at the start of the first pass:
+//   lb0  its lower bound of d2 to the nearest point outside its component;
+//   clb  the smallest such bound among its component's dirty points;
+//   cb   the best edge key its component holds so far (inf: none);
+//   ext2 squared diagonal of its leaf's box (local spacing);
+//   own_full its whole leaf is in its component;  round (1-based).
+__device__ __forceinline__ void features(float lb0, float clb, float cb, float ext2, bool own_full, int round,
+                                         float (&f)[kIn])
+{
+    const bool has_cb = cb < INFINITY;
+    f[0] = lg8(lb0);
+    f[1] = lg8(clb);
+    f[2] = has_cb ? lg8(cb) : 0.f;
+    f[3] = has_cb ? 1.f : 0.f;
+    f[4] = lg8(ext2);
+    f[5] = own_full ? 1.f : 0.f;
+    f[6] = 0.125f * (float)round;
+    f[7] = f[0] - f[1];
+}
+
+// Warp-wide inference: lane l's features (row l of a 32 x 8 batch) in, its
+// two outputs out.  All 32 lanes must call it together.  stage: 32 x 8 bf16
+// (512 bytes) of shared memory private to the warp; outs: 64 floats, also
+// private.  Layer outputs go from accumulator to operand registers directly
+// (an m16n8 accumulator pair is the m16k16 operand of the next layer).
+__device__ __forceinline__ void infer_warp(const Frag& W, const float (&f)[kIn], __nv_bfloat16* stage, float* outs,
+                                           float& o0, float& o1)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    uint32_t* s32 = reinterpret_cast<uint32_t*>(stage);  // row r: 4 words
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s32[lane * 4 + k] = pack_bf16(f[2 * k], f[2 * k + 1]);
+    __syncwarp();
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {  // rows mt*16 + {g, g+8}, one m-tile through all layers
+        // layer 1: input columns 2t, 2t+1 (8..15 are zero)
+        const uint32_t x0 = s32[(mt * 16 + g) * 4 + t], x1 = s32[(mt * 16 + g + 8) * 4 + t];
+        float h1[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float bl = W.b1[8 * j + 2 * t], bh = W.b1[8 * j + 2 * t + 1];
+            h1[j][0] = bl, h1[j][1] = bh, h1[j][2] = bl, h1[j][3] = bh;
+            mma16816(h1[j], x0, x1, 0u, 0u, W.w1[j][lane], 0u);
+        }
+        // layer 2: the accumulator pair (2q, 2q+1) is the operand of k-tile q
+        float h2[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float bl = W.b2[8 * j + 2 * t], bh = W.b2[8 * j + 2 * t + 1];
+            h2[j][0] = bl, h2[j][1] = bh, h2[j][2] = bl, h2[j][3] = bh;
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t a0 = pack_bf16(fmaxf(h1[2 * q][0], 0.f), fmaxf(h1[2 * q][1], 0.f));
+            const uint32_t a1 = pack_bf16(fmaxf(h1[2 * q][2], 0.f), fmaxf(h1[2 * q][3], 0.f));
+            const uint32_t a2 = pack_bf16(fmaxf(h1[2 * q + 1][0], 0.f), fmaxf(h1[2 * q + 1][1], 0.f));
+            const uint32_t a3 = pack_bf16(fmaxf(h1[2 * q + 1][2], 0.f), fmaxf(h1[2 * q + 1][3], 0.f));
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint2 b = W.w2[j][q][lane];
+                mma16816(h2[j], a0, a1, a2, a3, b.x, b.y);
+            }
+        }
+        // layer 3: 2 outputs in columns 0, 1 of one n-tile
+        float o[4] = {W.b3[2 * t], W.b3[2 * t + 1], W.b3[2 * t], W.b3[2 * t + 1]};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t a0 = pack_bf16(fmaxf(h2[2 * q][0], 0.f), fmaxf(h2[2 * q][1], 0.f));
+            const uint32_t a1 = pack_bf16(fmaxf(h2[2 * q][2], 0.f), fmaxf(h2[2 * q][3], 0.f));
+            const uint32_t a2 = pack_bf16(fmaxf(h2[2 * q + 1][0], 0.f), fmaxf(h2[2 * q + 1][1], 0.f));
+            const uint32_t a3 = pack_bf16(fmaxf(h2[2 * q + 1][2], 0.f), fmaxf(h2[2 * q + 1][3], 0.f));
+            const uint2 b = W.w3[q][lane];
+            mma16816(o, a0, a1, a2, a3, b.x, b.y);
+        }
+        if (t == 0) {
+            outs[2 * (mt * 16 + g)] = o[0];
+            outs[2 * (mt * 16 + g) + 1] = o[1];
+            outs[2 * (mt * 16 + g + 8)] = o[2];
+            outs[2 * (mt * 16 + g + 8) + 1] = o[3];
+        }
+    }
+    __syncwarp();
+    o0 = outs[2 * lane];
+    o1 = outs[2 * lane + 1];
+    __syncwarp();
+}
+
+}  // namespace prop
+
+}  // namespace emst

@@ -40,7 +40,18 @@ class Profile(ctypes.Structure):
                 ("ms_resolve", ctypes.c_double), ("ms_hook", ctypes.c_double), ("ms_flatten", ctypes.c_double),
                 ("launches", ctypes.c_int64), ("octant_launches", ctypes.c_int64), ("rounds", ctypes.c_int64),
                 ("leaf_visits", ctypes.c_int64), ("node_tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
-                ("search_warps", ctypes.c_int64), ("search_queries", ctypes.c_int64)]
+                ("search_warps", ctypes.c_int64), ("search_queries", ctypes.c_int64),
+                ("first_pass_searches", ctypes.c_int64), ("first_pass_resumed", ctypes.c_int64),
+                ("first_pass_deferred", ctypes.c_int64)]
+
+
+class TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_int), ("batch", ctypes.c_int), ("lr", ctypes.c_float),
+                ("reg_weight", ctypes.c_float), ("seed", ctypes.c_uint64), ("device", ctypes.c_int)]
+
+
+PROPOSAL_WEIGHTS = 1410
+TRACE_RECORD = 12
 
 
 def build(jobs=4):
@@ -77,6 +88,10 @@ def lib():
             "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
             "emst_search_shape_info": [P, P, P, I], "emst_autotune": [P, P, i64, I, P, P, I],
             "emst_get_search_shape": [P, P],
+            "emst_set_proposal": [P, P, ctypes.c_float], "emst_trace_enable": [P, i64, I],
+            "emst_get_trace": [P, P, i64, P], "emst_get_trace_device": [P, P, P],
+            "emst_proposal_init": [ctypes.c_uint64, P], "emst_proposal_train": [P, i64, I, P, P, P],
+            "emst_proposal_grad": [P, P, i64, ctypes.c_float, P, P],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -96,6 +111,42 @@ def search_shapes():
     m = np.zeros(cnt.value, np.int32)
     lib().emst_search_shape_info(ctypes.byref(cnt), _p(t), _p(m), cnt.value)
     return cnt.value, t, m
+
+
+def proposal_init(seed=0):
+    w = np.zeros(PROPOSAL_WEIGHTS, np.float32)
+    lib().emst_proposal_init(ctypes.c_uint64(seed), _p(w))
+    return w
+
+
+def proposal_train(records, weights, epochs=4, batch=4096, lr=2e-3, reg_weight=1.0, seed=0, device=0,
+                   records_on_device=None, n_records=None):
+    """Trains on trace records (host array, or device pointer + n_records) with the
+    library's tensor-core kernels. -> (trained weights, mean loss per epoch)."""
+    w = np.ascontiguousarray(weights, np.float32).copy()
+    cfg = TrainConfig(int(epochs), int(batch), float(lr), float(reg_weight), int(seed), int(device))
+    curve = np.zeros(max(int(epochs), 1), np.float32)
+    if records_on_device is not None:
+        st = lib().emst_proposal_train(ctypes.c_void_p(records_on_device), int(n_records), 1, ctypes.byref(cfg),
+                                       _p(w), _p(curve))
+    else:
+        r = np.ascontiguousarray(records, np.float32)
+        st = lib().emst_proposal_train(_p(r), len(r), 0, ctypes.byref(cfg), _p(w), _p(curve))
+    if st != 0:
+        raise EmstError(st, "emst_proposal_train failed")
+    return w, curve
+
+
+def proposal_grad(weights, records, reg_weight=1.0):
+    """One GPU forward/backward: (gradient of the mean loss, loss)."""
+    w = np.ascontiguousarray(weights, np.float32)
+    r = np.ascontiguousarray(records, np.float32)
+    g = np.zeros(PROPOSAL_WEIGHTS, np.float32)
+    loss = ctypes.c_float()
+    st = lib().emst_proposal_grad(_p(w), _p(r), len(r), float(reg_weight), _p(g), ctypes.byref(loss))
+    if st != 0:
+        raise EmstError(st, "emst_proposal_grad failed")
+    return g, loss.value
 
 
 def _p(a):
@@ -274,6 +325,34 @@ class Emst:
         v = ctypes.c_int()
         self._chk(lib().emst_get_search_shape(self.h, ctypes.byref(v)))
         return v.value
+
+    # --- learned proposal ------------------------------------------------
+    def set_proposal(self, weights, margin=1.0):
+        """weights: PROPOSAL_WEIGHTS floats (learned first pass on) or None (off)."""
+        if weights is None:
+            self._chk(lib().emst_set_proposal(self.h, None, 0.0))
+            return
+        w = np.ascontiguousarray(weights, np.float32).ravel()
+        assert w.size == PROPOSAL_WEIGHTS
+        self._chk(lib().emst_set_proposal(self.h, _p(w), float(margin)))
+
+    def trace_enable(self, capacity, sample_shift=0):
+        self._chk(lib().emst_trace_enable(self.h, int(capacity), int(sample_shift)))
+
+    def trace(self):
+        """Trace records so far, (count, TRACE_RECORD) float32."""
+        cnt = ctypes.c_int64()
+        self._chk(lib().emst_get_trace(self.h, None, 0, ctypes.byref(cnt)))
+        out = np.zeros((cnt.value, TRACE_RECORD), np.float32)
+        if cnt.value:
+            self._chk(lib().emst_get_trace(self.h, _p(out), cnt.value, ctypes.byref(cnt)))
+        return out
+
+    def trace_device(self):
+        """(device pointer, count) of the trace records."""
+        ptr, cnt = ctypes.c_void_p(), ctypes.c_int64()
+        self._chk(lib().emst_get_trace_device(self.h, ctypes.byref(ptr), ctypes.byref(cnt)))
+        return ptr.value, cnt.value
 
     def solve_device(self, d_points, n, dim, d_uv, d_length):
         ne = ctypes.c_int64()

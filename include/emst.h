@@ -82,6 +82,13 @@ typedef struct {
     int64_t candidates;
     int64_t search_warps;
     int64_t search_queries; /* component mode: point searches run (all rounds) */
+    /* component mode, first search pass: searches run, of those the ones cut
+     * short by the learned radius and searched again in the second pass (the
+     * proposal's mispredictions), and points sent to the second pass
+     * without a first search */
+    int64_t first_pass_searches;
+    int64_t first_pass_resumed;
+    int64_t first_pass_deferred;
 } emst_profile;
 
 /* Context lifetime.  Replaces CalculateurEMST::initialize / the static
@@ -205,6 +212,59 @@ emst_status emst_solve_batch(emst_ctx* ctx, const float* points, const int64_t* 
  * termination read. */
 emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
                               double* d_length, int64_t* n_edges);
+
+/* ---------------------------------------------------------------------------
+ * Learned search proposal (no counterpart in the reference; it stands beside
+ * the plain search and leaves its results unchanged)
+ *
+ * A small network (8 inputs, two hidden layers of 32, 2 outputs; BF16
+ * tensor-core inference fused into the search kernel) predicts, for each
+ * point about to search, the radius its component's shortest outgoing edge
+ * will have and whether this point can hold that edge.  The first search
+ * pass follows the prediction: points predicted not to hold it wait for the
+ * second pass, the others search only up to the predicted radius (times
+ * 2^margin in d2).  A search the radius cut short keeps a certified lower
+ * bound and runs again in the second pass, whose searches use the
+ * component's real bound, so the edge set is the plain method's.
+ * ------------------------------------------------------------------------- */
+
+#define EMST_PROPOSAL_WEIGHTS 1410 /* W1[8][32] b1[32] W2[32][32] b2[32] W3[32][2] b3[2], FP32 */
+#define EMST_TRACE_RECORD 12       /* floats per trace record */
+
+/* Turns the learned first pass on (weights: EMST_PROPOSAL_WEIGHTS floats)
+ * or off (weights NULL).  margin: log2 factor on the predicted radius, in
+ * [0, 64].  Single-cloud solves only (batches keep the plain rule). */
+emst_status emst_set_proposal(emst_ctx* ctx, const float* weights, float margin);
+
+/* Training traces: from now on, solves of this context (plain first pass)
+ * record 1 in 2^sample_shift first-pass queries, up to `capacity` records in
+ * total (capacity 0: off).  Record: 8 features, log2(d2 of the component's
+ * shortest edge)/8, [point's lower bound <= that d2], 1 if the component had
+ * an edge (else the regression target is void), the component label bits. */
+emst_status emst_trace_enable(emst_ctx* ctx, int64_t capacity, int sample_shift);
+emst_status emst_get_trace(emst_ctx* ctx, float* records, int64_t cap, int64_t* count);
+emst_status emst_get_trace_device(emst_ctx* ctx, const float** d_records, int64_t* count);
+
+typedef struct {
+    int epochs;       /* passes over the records (0: 4) */
+    int batch;        /* records per Adam step (0: 4096) */
+    float lr;         /* Adam step size (0: 2e-3) */
+    float reg_weight; /* radius loss weight against the class loss (0: 1) */
+    uint64_t seed;    /* record order */
+    int device;
+} emst_train_config;
+
+/* Seeded initial weights (uniform, fan-in scaled). */
+emst_status emst_proposal_init(uint64_t seed, float* weights);
+/* Trains the proposal on trace records (host or device) with the library's
+ * BF16 tensor-core forward/backward kernels and Adam; weights in (initial)
+ * and out (trained); loss_curve (optional): mean loss per epoch. */
+emst_status emst_proposal_train(const float* records, int64_t n_records, int records_on_device,
+                                const emst_train_config* cfg, float* weights, float* loss_curve);
+/* One forward/backward over host records: gradient of the mean loss
+ * (EMST_PROPOSAL_WEIGHTS floats) and the loss, for checking. */
+emst_status emst_proposal_grad(const float* weights, const float* records, int64_t n_records, float reg_weight,
+                               float* grad, float* loss);
 
 /* ---------------------------------------------------------------------------
  * Launch-shape autotuner (no counterpart in the reference, whose kernels use
