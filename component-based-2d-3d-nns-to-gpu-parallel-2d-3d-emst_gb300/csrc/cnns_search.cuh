@@ -278,7 +278,11 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 selkey[me] = key;
                 if (key <= __ldcg(&ckey[labp])) {
                     const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
-                    record = old >= key;
+                    // a result the second pass will redo still bounds the
+                    // component's key, but only its second search may list
+                    // the point as a provisional winner (at most once a round:
+                    // the list holds n entries)
+                    record = old >= key && !again;
                 }
             } else {
                 selq[me] = kNone;
