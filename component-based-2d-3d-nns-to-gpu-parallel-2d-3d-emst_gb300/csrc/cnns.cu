@@ -417,7 +417,7 @@ cudaError_t cnns_select(Ctx& c)
             CnnsArgs a{c.spl.p,  c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
                        cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
                        c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
-                       &d->round};
+                       c.threshold, &d->round};
             const int shape = search_shape_of(c);
             const bool learned = c.learned && pass == 1 && !pc;
             if (pass == 1 && c.trace_cap > 0 && !learned) {

@@ -65,21 +65,10 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     const uint32_t* __restrict__ ncloud = a.ncloud;
     unsigned long long* __restrict__ stats = a.stats;
     constexpr int kTStack = 48;
-    constexpr int kWarps = TPB / 32;
-    __shared__ __align__(16) unsigned char s_prop[LEARN ? sizeof(prop::Frag) + kWarps * (512 + 256) : 16];
-    prop::Frag& W = *reinterpret_cast<prop::Frag*>(s_prop);
-    __nv_bfloat16* s_stage = nullptr;
-    float* s_outs = nullptr;
-    int round = 0;
-    if constexpr (LEARN) {
-        s_stage = reinterpret_cast<__nv_bfloat16*>(s_prop + sizeof(prop::Frag)) + (threadIdx.x >> 5) * 256;
-        s_outs = reinterpret_cast<float*>(s_prop + sizeof(prop::Frag) + kWarps * 512) + (threadIdx.x >> 5) * 64;
-        const uint4* src = reinterpret_cast<const uint4*>(a.frag);
-        uint4* dst = reinterpret_cast<uint4*>(s_prop);
-        for (int i = threadIdx.x; i < (int)(sizeof(prop::Frag) / 16); i += TPB) dst[i] = src[i];
-        round = *a.round;
-        __syncthreads();
-    }
+    // learned proposal: weights stay in global memory (read-only cache); the
+    // kernel uses no shared memory, so the SM keeps its whole L1 for the search
+    const prop::Frag* W = reinterpret_cast<const prop::Frag*>(a.frag);
+    const int round = LEARN ? *a.round : 0;
     const uint32_t total = *n_list;
     for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
         const uint32_t qi = base0 + threadIdx.x;
@@ -110,10 +99,10 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 for (int i = 0; i < prop::kIn; ++i) f[i] = 0.f;
             }
             float o0, o1;
-            prop::infer_warp(W, f, s_stage, s_outs, o0, o1);
+            prop::infer_warp(W, f, o0, o1);
             if (valid) {
                 cap = exp2f(fminf(8.f * o0 + a.margin, 126.f));
-                if (o1 < 0.f || cap < lb0) {
+                if (o1 < a.threshold || cap < lb0) {
                     valid = false;  // predicted not to hold the minimum: second pass
                     deferred = true;
                 }

@@ -814,7 +814,7 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
     return read_counters(x);
 }
 
-emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin)
+emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin, float threshold)
 {
     if (!x) return EMST_EINVAL;
     Ctx& c = x->c;
@@ -825,6 +825,7 @@ emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin)
     if (c.search_mode != 0 || c.cnns_warp)
         return set_err(x, EMST_EINVAL, "the learned proposal drives the component search (search_mode 0)");
     if (!(margin >= 0.f && margin <= 64.f)) return set_err(x, EMST_EINVAL, "margin must be in [0, 64]");
+    if (!std::isfinite(threshold)) return set_err(x, EMST_EINVAL, "threshold must be finite");
     for (int i = 0; i < emst::prop::kNumWeights; ++i)
         if (!std::isfinite(weights[i])) return set_err(x, EMST_EINVAL, "non-finite proposal weight");
     EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
@@ -836,6 +837,7 @@ emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin)
     EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
     c.learned = true;
     c.margin = margin;
+    c.threshold = threshold;
     return EMST_OK;
 }
 

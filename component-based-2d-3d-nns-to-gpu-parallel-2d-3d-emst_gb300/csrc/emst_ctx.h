@@ -141,6 +141,7 @@ struct Ctx {
     // learned proposal (proposal.cuh): packed weights, radius margin (log2)
     bool learned = false;
     float margin = 1.f;
+    float threshold = 0.f;
     DevBuf<unsigned char> pfrag;
     // search traces for training: records of prop::kRec floats, 1 in 2^shift
     // first-pass queries; ctl = {records written, first record of the round}
@@ -209,6 +210,7 @@ struct CnnsArgs {
     unsigned long long* stats;
     const void* frag;  // learned proposal: fragment-ordered weights (prop::Frag), or null
     float margin;      // learned proposal: log2 margin added to the predicted radius
+    float threshold;   // learned proposal: class logit at or above which a point searches first
     const int* round;  // rounds started (device)
 };
 

@@ -1,9 +1,9 @@
 // proposal.cu -- the learned proposal's data and training on the GPU:
 //
 //   * traces: while the plain method runs, sampled first-pass queries record
-//     their features; after the round, the label -- the d2 of the shortest
-//     edge their component actually got, and whether the point's lower bound
-//     allowed it to hold that edge;
+//     their features; after the round, the labels -- the d2 of the shortest
+//     edge their component actually got, and whether the point's own search
+//     found that edge (it is its component's winner);
 //   * training: forward and backward of the 8-32-32-2 MLP with BF16 MMA
 //     (m16n8k16, FP32 accumulate), FP32 master weights and Adam;
 //   * packing: FP32 weights into the fragment order of the fused inference.
@@ -107,32 +107,32 @@ __global__ void k_trace_features(const uint32_t* __restrict__ list, const uint32
         float* o = rec + (uint64_t)at * kRec;
         for (int j = 0; j < kIn; ++j) o[j] = f[j];
         o[8] = 0.f;
-        o[9] = lb0;  // replaced by the class label after the round
-        o[10] = -1.f;
+        o[9] = 0.f;
+        o[10] = __uint_as_float(me);  // replaced by the regression mask after the round
         o[11] = __uint_as_float(labp);
     }
 }
 
-// After the round: each of this round's records gets its component's final
-// shortest edge (regression target, masked when there is none) and whether
-// its lower bound was at most that edge (class label).
-__global__ void k_trace_labels(const uint64_t* __restrict__ ckey, float* __restrict__ rec,
-                               const uint32_t* __restrict__ ctl, uint64_t cap)
+// After the round's searches: each of this round's records gets its
+// component's final shortest edge (regression target, masked when there is
+// none) and whether the point's own search found exactly that edge (class
+// label: the point is its component's winner).
+__global__ void k_trace_labels(const uint64_t* __restrict__ ckey, const uint64_t* __restrict__ selkey,
+                               float* __restrict__ rec, const uint32_t* __restrict__ ctl, uint64_t cap)
 {
     const uint64_t first = ctl[1], last = min((uint64_t)ctl[0], cap);
     for (uint64_t i = first + blockIdx.x * blockDim.x + threadIdx.x; i < last; i += (uint64_t)gridDim.x * blockDim.x) {
         float* o = rec + i * kRec;
         const uint32_t labp = __float_as_uint(o[11]);
+        const uint32_t me = __float_as_uint(o[10]);
         const uint64_t k = ckey[labp];
-        const float lb0 = o[9];
         if (k == kNoKey) {
             o[8] = 0.f;
             o[9] = 0.f;
             o[10] = 0.f;
         } else {
-            const float cbf = __uint_as_float((uint32_t)(k >> 32));
-            o[8] = prop::lg8(cbf);
-            o[9] = lb0 <= cbf ? 1.f : 0.f;
+            o[8] = prop::lg8(__uint_as_float((uint32_t)(k >> 32)));
+            o[9] = selkey[me] == k ? 1.f : 0.f;
             o[10] = 1.f;
         }
     }
@@ -380,7 +380,8 @@ cudaError_t proposal_trace_begin(Ctx& c)
 
 cudaError_t proposal_trace_end(Ctx& c)
 {
-    k_trace_labels<<<c.sms * 4, 256, 0, c.stream>>>(c.ckey.p, c.trace.p, c.trace_ctl.p, (uint64_t)c.trace_cap);
+    k_trace_labels<<<c.sms * 4, 256, 0, c.stream>>>(c.ckey.p, c.selkey.p, c.trace.p, c.trace_ctl.p,
+                                                   (uint64_t)c.trace_cap);
     c.launches++;
     return cudaGetLastError();
 }

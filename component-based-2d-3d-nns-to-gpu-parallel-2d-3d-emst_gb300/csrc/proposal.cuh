@@ -8,8 +8,10 @@
 // For each dirty point it predicts
 //   out0: log2(d2 of its component's shortest outgoing edge) / 8 -- the
 //         search radius: the first-pass search stops at that radius;
-//   out1: logit of "this point can hold the component's minimum" -- the
-//         visit order: points below 0 wait for the second pass.
+//   out1: logit of "this point's search finds its component's minimum" --
+//         the visit order: points below a threshold wait for the second
+//         pass, where the component's bound, tightened by the first pass,
+//         cuts their searches short.
 // Neither output changes what is found.  A first-pass search cut short by
 // the radius leaves a certified lower bound and goes to the second pass,
 // which searches with the component's real bound, so every component's
@@ -27,7 +29,8 @@ constexpr int kIn = 8, kHid = 32, kOut = 2;
 // FP32 master weights, row-major [in][out]: W1 b1 W2 b2 W3 b3.
 constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kIn * kHid, kOffW2 = kOffB1 + kHid, kOffB2 = kOffW2 + kHid * kHid,
               kOffW3 = kOffB2 + kHid, kOffB3 = kOffW3 + kHid * kOut, kNumWeights = kOffB3 + kOut;  // 1410
-// Trace record: 8 features, regression target, class label, regression mask, spare.
+// Trace record: 8 features, regression target, class label, regression mask,
+// component label bits.
 constexpr int kRec = 12;
 
 // Fragment-ordered BF16 weights for the fused inference, one 32-bit register
@@ -81,35 +84,42 @@ __device__ __forceinline__ void features(float lb0, float clb, float cb, float e
 }
 
 // Warp-wide inference: lane l's features (row l of a 32 x 8 batch) in, its
-// two outputs out.  All 32 lanes must call it together.  stage: 32 x 8 bf16
-// (512 bytes) of shared memory private to the warp; outs: 64 floats, also
-// private.  Layer outputs go from accumulator to operand registers directly
-// (an m16n8 accumulator pair is the m16k16 operand of the next layer).
-__device__ __forceinline__ void infer_warp(const Frag& W, const float (&f)[kIn], __nv_bfloat16* stage, float* outs,
-                                           float& o0, float& o1)
+// two outputs out.  All 32 lanes must call it together.  W: the weights in
+// global memory (read through the read-only cache).  No shared memory: rows
+// move between lanes by shuffles, and layer outputs go from accumulator to
+// operand registers directly (an m16n8 accumulator pair is the m16k16
+// operand of the next layer).
+__device__ __forceinline__ void infer_warp(const Frag* __restrict__ W, const float (&f)[kIn], float& o0, float& o1)
 {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    uint32_t* s32 = reinterpret_cast<uint32_t*>(stage);  // row r: 4 words
+    uint32_t w[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) s32[lane * 4 + k] = pack_bf16(f[2 * k], f[2 * k + 1]);
-    __syncwarp();
+    for (int k = 0; k < 4; ++k) w[k] = pack_bf16(f[2 * k], f[2 * k + 1]);
+    float out[2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {  // rows mt*16 + {g, g+8}, one m-tile through all layers
-        // layer 1: input columns 2t, 2t+1 (8..15 are zero)
-        const uint32_t x0 = s32[(mt * 16 + g) * 4 + t], x1 = s32[(mt * 16 + g + 8) * 4 + t];
+        // layer 1: word t (input columns 2t, 2t+1) of rows g and g+8; 8..15 are zero
+        uint32_t x0 = 0, x1 = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t v0 = __shfl_sync(full, w[k], mt * 16 + g);
+            const uint32_t v1 = __shfl_sync(full, w[k], mt * 16 + g + 8);
+            if (k == t) x0 = v0, x1 = v1;
+        }
         float h1[4][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float bl = W.b1[8 * j + 2 * t], bh = W.b1[8 * j + 2 * t + 1];
-            h1[j][0] = bl, h1[j][1] = bh, h1[j][2] = bl, h1[j][3] = bh;
-            mma16816(h1[j], x0, x1, 0u, 0u, W.w1[j][lane], 0u);
+            const float2 bb = __ldg(reinterpret_cast<const float2*>(&W->b1[8 * j + 2 * t]));
+            h1[j][0] = bb.x, h1[j][1] = bb.y, h1[j][2] = bb.x, h1[j][3] = bb.y;
+            mma16816(h1[j], x0, x1, 0u, 0u, __ldg(&W->w1[j][lane]), 0u);
         }
         // layer 2: the accumulator pair (2q, 2q+1) is the operand of k-tile q
         float h2[4][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float bl = W.b2[8 * j + 2 * t], bh = W.b2[8 * j + 2 * t + 1];
-            h2[j][0] = bl, h2[j][1] = bh, h2[j][2] = bl, h2[j][3] = bh;
+            const float2 bb = __ldg(reinterpret_cast<const float2*>(&W->b2[8 * j + 2 * t]));
+            h2[j][0] = bb.x, h2[j][1] = bb.y, h2[j][2] = bb.x, h2[j][3] = bb.y;
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -119,32 +129,35 @@ __device__ __forceinline__ void infer_warp(const Frag& W, const float (&f)[kIn],
             const uint32_t a3 = pack_bf16(fmaxf(h1[2 * q + 1][2], 0.f), fmaxf(h1[2 * q + 1][3], 0.f));
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint2 b = W.w2[j][q][lane];
+                const uint2 b = __ldg(&W->w2[j][q][lane]);
                 mma16816(h2[j], a0, a1, a2, a3, b.x, b.y);
             }
         }
         // layer 3: 2 outputs in columns 0, 1 of one n-tile
-        float o[4] = {W.b3[2 * t], W.b3[2 * t + 1], W.b3[2 * t], W.b3[2 * t + 1]};
+        const float2 b3 = __ldg(reinterpret_cast<const float2*>(&W->b3[2 * t]));
+        float o[4] = {b3.x, b3.y, b3.x, b3.y};
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const uint32_t a0 = pack_bf16(fmaxf(h2[2 * q][0], 0.f), fmaxf(h2[2 * q][1], 0.f));
             const uint32_t a1 = pack_bf16(fmaxf(h2[2 * q][2], 0.f), fmaxf(h2[2 * q][3], 0.f));
             const uint32_t a2 = pack_bf16(fmaxf(h2[2 * q + 1][0], 0.f), fmaxf(h2[2 * q + 1][1], 0.f));
             const uint32_t a3 = pack_bf16(fmaxf(h2[2 * q + 1][2], 0.f), fmaxf(h2[2 * q + 1][3], 0.f));
-            const uint2 b = W.w3[q][lane];
+            const uint2 b = __ldg(&W->w3[q][lane]);
             mma16816(o, a0, a1, a2, a3, b.x, b.y);
         }
-        if (t == 0) {
-            outs[2 * (mt * 16 + g)] = o[0];
-            outs[2 * (mt * 16 + g) + 1] = o[1];
-            outs[2 * (mt * 16 + g + 8)] = o[2];
-            outs[2 * (mt * 16 + g + 8) + 1] = o[3];
-        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) out[mt][i] = o[i];
     }
-    __syncwarp();
-    o0 = outs[2 * lane];
-    o1 = outs[2 * lane + 1];
-    __syncwarp();
+    // row r's outputs sit in lane 4 * (r & 7) (t = 0): registers 0, 1 for
+    // rows 0..7 of its m-tile, 2, 3 for rows 8..15
+    const int src = 4 * (lane & 7), mt = lane >> 4, half = (lane >> 3) & 1;
+    float r[2][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) r[m][i] = __shfl_sync(full, out[m][i], src);
+    o0 = mt ? (half ? r[1][2] : r[1][0]) : (half ? r[0][2] : r[0][0]);
+    o1 = mt ? (half ? r[1][3] : r[1][1]) : (half ? r[0][3] : r[0][1]);
 }
 
 }  // namespace prop

@@ -88,7 +88,7 @@ def lib():
             "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
             "emst_search_shape_info": [P, P, P, I], "emst_autotune": [P, P, i64, I, P, P, I],
             "emst_get_search_shape": [P, P],
-            "emst_set_proposal": [P, P, ctypes.c_float], "emst_trace_enable": [P, i64, I],
+            "emst_set_proposal": [P, P, ctypes.c_float, ctypes.c_float], "emst_trace_enable": [P, i64, I],
             "emst_get_trace": [P, P, i64, P], "emst_get_trace_device": [P, P, P],
             "emst_proposal_init": [ctypes.c_uint64, P], "emst_proposal_train": [P, i64, I, P, P, P],
             "emst_proposal_grad": [P, P, i64, ctypes.c_float, P, P],
@@ -327,14 +327,14 @@ class Emst:
         return v.value
 
     # --- learned proposal ------------------------------------------------
-    def set_proposal(self, weights, margin=1.0):
+    def set_proposal(self, weights, margin=1.0, threshold=0.0):
         """weights: PROPOSAL_WEIGHTS floats (learned first pass on) or None (off)."""
         if weights is None:
-            self._chk(lib().emst_set_proposal(self.h, None, 0.0))
+            self._chk(lib().emst_set_proposal(self.h, None, 0.0, 0.0))
             return
         w = np.ascontiguousarray(weights, np.float32).ravel()
         assert w.size == PROPOSAL_WEIGHTS
-        self._chk(lib().emst_set_proposal(self.h, _p(w), float(margin)))
+        self._chk(lib().emst_set_proposal(self.h, _p(w), float(margin), float(threshold)))
 
     def trace_enable(self, capacity, sample_shift=0):
         self._chk(lib().emst_trace_enable(self.h, int(capacity), int(sample_shift)))

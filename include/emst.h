@@ -220,12 +220,14 @@ emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, i
  * A small network (8 inputs, two hidden layers of 32, 2 outputs; BF16
  * tensor-core inference fused into the search kernel) predicts, for each
  * point about to search, the radius its component's shortest outgoing edge
- * will have and whether this point can hold that edge.  The first search
- * pass follows the prediction: points predicted not to hold it wait for the
- * second pass, the others search only up to the predicted radius (times
- * 2^margin in d2).  A search the radius cut short keeps a certified lower
- * bound and runs again in the second pass, whose searches use the
- * component's real bound, so the edge set is the plain method's.
+ * will have and how likely this point's own search is to find that edge.
+ * The first search pass follows the prediction: points below the threshold
+ * wait for the second pass (where the component's bound, tightened by the
+ * first pass, cuts their searches short), the others search only up to the
+ * predicted radius (times 2^margin in d2).  A search the radius cut short
+ * keeps a certified lower bound and runs again in the second pass, whose
+ * searches use the component's real bound, so the edge set is the plain
+ * method's.
  * ------------------------------------------------------------------------- */
 
 #define EMST_PROPOSAL_WEIGHTS 1410 /* W1[8][32] b1[32] W2[32][32] b2[32] W3[32][2] b3[2], FP32 */
@@ -233,14 +235,16 @@ emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, i
 
 /* Turns the learned first pass on (weights: EMST_PROPOSAL_WEIGHTS floats)
  * or off (weights NULL).  margin: log2 factor on the predicted radius, in
- * [0, 64].  Single-cloud solves only (batches keep the plain rule). */
-emst_status emst_set_proposal(emst_ctx* ctx, const float* weights, float margin);
+ * [0, 64]; threshold: class logit at or above which a point searches in the
+ * first pass.  Single-cloud solves only (batches keep the plain rule). */
+emst_status emst_set_proposal(emst_ctx* ctx, const float* weights, float margin, float threshold);
 
 /* Training traces: from now on, solves of this context (plain first pass)
  * record 1 in 2^sample_shift first-pass queries, up to `capacity` records in
  * total (capacity 0: off).  Record: 8 features, log2(d2 of the component's
- * shortest edge)/8, [point's lower bound <= that d2], 1 if the component had
- * an edge (else the regression target is void), the component label bits. */
+ * shortest edge)/8, [the point's own search found that edge], 1 if the
+ * component had an edge (else both targets are void), the component label
+ * bits. */
 emst_status emst_trace_enable(emst_ctx* ctx, int64_t capacity, int sample_shift);
 emst_status emst_get_trace(emst_ctx* ctx, float* records, int64_t cap, int64_t* count);
 emst_status emst_get_trace_device(emst_ctx* ctx, const float** d_records, int64_t* count);

@@ -62,7 +62,7 @@ def test_traces_are_well_formed(gpu_lib):
     assert rec[:, 10].mean() > 0.99  # every component but the last has an edge
     rounds = np.round(rec[:, 6] * 8).astype(int)
     assert rounds.min() == 1 and rounds.max() >= 5
-    assert rec[rounds == 1, 9].mean() == 1.0  # in round 1 every lower bound is 0
+    assert rec[rounds == 1, 9].mean() == 1.0  # in round 1 every point is its own component's winner
     # sampling: shift 2 keeps about half as many records as shift 1
     rec2 = _traces(gpu_lib, clouds, shift=2)
     assert 0.35 < len(rec2) / len(rec) < 0.65
