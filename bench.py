@@ -230,7 +230,11 @@ def main():
     d_uv = torch.empty((max(n - 1, 1), 2), dtype=torch.int32, device="cuda")
     d_len = torch.empty(1, dtype=torch.float64, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # one dedicated stream for torch's work (inputs, the L2 flush, events) and the
+    # library's, so that every step is ordered after the previous one
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()  # inputs above were made on the default stream
+    torch.cuda.set_stream(stream)
     # timed context: the default path (the component search runs its round loop
     # as one CUDA graph); a separate profiled context (host-driven rounds with
     # per-phase CUDA events) gives the phase split and the kernel times

@@ -312,6 +312,62 @@ __global__ void k_pack_spl(uint32_t n, const float4* __restrict__ sp, const uint
     spl[i] = v;
 }
 
+// Who searches in the first pass (flag 1), who waits for the second (2), who
+// needs no search this round (0), decided before the search so that search
+// warps carry only real searches.  A dirty point whose lower bound exceeds
+// its component's key (set by reused partners) cannot hold the minimum; one
+// whose bound exceeds `factor` times its component's smallest waits.
+__global__ void k_filter_first(uint32_t n, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
+                               const float* __restrict__ lbp, const uint64_t* __restrict__ ckey,
+                               const uint32_t* __restrict__ clb, float factor, unsigned long long* __restrict__ stats)
+{
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t p = base + threadIdx.x;
+        bool later = false;
+        if (p < n && flag[p]) {
+            const uint32_t l = lab[p];
+            const float lb = lbp[p];
+            const uint64_t k = __ldcg(&ckey[l]);
+            const float cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+            later = !(lb > cb) && lb > factor * __uint_as_float(__ldcg(&clb[l]));
+            flag[p] = lb > cb ? 0 : (later ? 2 : 1);
+        }
+        if (stats) {
+            const unsigned m = __ballot_sync(kFull, later);
+            if ((threadIdx.x & 31) == 0 && m) atomicAdd(&stats[7], (unsigned long long)__popc(m));
+        }
+    }
+}
+
+// Second-pass searchers: waiting points (2) whose bound the first pass did
+// not rule out.
+__global__ void k_filter_second(uint32_t n, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
+                                const float* __restrict__ lbp, const uint64_t* __restrict__ ckey)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const unsigned char f = flag[p];
+    if (!f) return;
+    bool go = false;
+    if (f == 2) {
+        const uint64_t k = __ldcg(&ckey[lab[p]]);
+        go = k == kNoKey || !(lbp[p] > __uint_as_float((uint32_t)(k >> 32)));
+    }
+    flag[p] = go ? 1 : 0;
+}
+
+struct FlagIsOne {
+    const unsigned char* f;
+    __host__ __device__ bool operator()(uint32_t i) const { return f[i] == 1; }
+};
+
+cudaError_t select_flagged_one(Ctx& c, uint32_t* out, uint32_t* count)
+{
+    size_t tb = c.sel_tmp.cap;
+    return cub::DeviceSelect::If(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), out, count, (int)c.n,
+                                 FlagIsOne{c.dflag.p}, c.stream);
+}
+
 __global__ void k_fill_u32(uint32_t* __restrict__ p, uint32_t n, uint32_t v)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -369,11 +425,14 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
     if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
     if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
-    size_t tb = 0;
+    size_t tb = 0, tb2 = 0;
     if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
                                         &c.ctr.p->n_dirty, (int)n, c.stream)) != cudaSuccess)
         return e;
-    if ((e = ensure(c.sel_tmp, tb)) != cudaSuccess) return e;
+    if ((e = cub::DeviceSelect::If(nullptr, tb2, thrust::counting_iterator<uint32_t>(0), c.dirty.p,
+                                   &c.ctr.p->n_dirty, (int)n, FlagIsOne{c.dflag.p}, c.stream)) != cudaSuccess)
+        return e;
+    if ((e = ensure(c.sel_tmp, std::max(tb, tb2))) != cudaSuccess) return e;
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
     cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
@@ -388,15 +447,25 @@ cudaError_t cnns_select(Ctx& c)
     DevCounters* d = c.ctr.p;  // n_dirty, n_dirty2, n_prov were zeroed by the round tick
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
                                                   c.clb.p, c.dflag.p, c.prov.p, &d->n_prov);
-    // dirty points in leaf order: a warp's 32 queries are neighbours, so their
+    // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
-    size_t tb = c.sel_tmp.cap;
-    cudaError_t e = cub::DeviceSelect::Flagged(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p,
-                                               c.dirty.p, &d->n_dirty, (int)c.n, c.stream);
+    cudaError_t e;
+    unsigned long long* st = c.profile ? c.nstats.p : nullptr;
+    if (c.cnns_warp) {
+        size_t tb = c.sel_tmp.cap;
+        e = cub::DeviceSelect::Flagged(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
+                                       &d->n_dirty, (int)c.n, c.stream);
+    } else {
+        // the learned proposal makes the first-pass choice itself
+        const float first_factor = c.learned && !c.n_clouds ? INFINITY : c.first_pass_factor;
+        k_filter_first<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
+                                                              c.clb.p, first_factor, st);
+        c.launches++;
+        e = select_flagged_one(c, c.dirty.p, &d->n_dirty);
+    }
     if (e != cudaSuccess) return e;
     constexpr int WPB = 4;
     const unsigned blocks = (unsigned)std::min<int64_t>((c.n + 32 * WPB - 1) / (32 * WPB), 152 * 32);
-    unsigned long long* st = c.profile ? c.nstats.p : nullptr;
     const uint32_t* pc = c.n_clouds ? c.pcloud.p : nullptr;
     const uint32_t* nc = c.n_clouds ? c.ncloud.p : nullptr;
     for (int pass = 1; pass <= 2; ++pass) {
@@ -428,9 +497,10 @@ cudaError_t cnns_select(Ctx& c)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
             if (pass == 1) {
-                size_t tbytes = c.sel_tmp.cap;
-                cudaError_t e2 = cub::DeviceSelect::Flagged(c.sel_tmp.p, tbytes, thrust::counting_iterator<uint32_t>(0),
-                                                            c.dflag.p, c.dirty2.p, &d->n_dirty2, (int)c.n, c.stream);
+                k_filter_second<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p,
+                                                                             c.lbp.p, c.ckey.p);
+                c.launches++;
+                cudaError_t e2 = select_flagged_one(c, c.dirty2.p, &d->n_dirty2);
                 if (e2 != cudaSuccess) return e2;
             }
         }

@@ -107,9 +107,6 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                     deferred = true;
                 }
             }
-        } else if (valid && pass == 1 && lb0 > 4.f * __uint_as_float(__ldcg(&clb[labp]))) {
-            valid = false;  // not among its component's most promising points: second pass
-            deferred = true;
         }
         bool again = false;  // first-pass search cut short by the proposal's radius
 
@@ -281,8 +278,8 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
         // lanes of a diverged warp drift into different iterations and the
         // next traversals run with a fraction of the warp active.
         __syncwarp();
-        // second-pass flags, compacted in leaf order after the first pass
-        if (listed && pass == 1) dflag[me] = (deferred || again) ? 1 : 0;
+        // second-pass candidates (2), compacted in leaf order after the first pass
+        if (listed && pass == 1) dflag[me] = (deferred || again) ? 2 : 0;
         warp_append(record, me, prov, n_prov);
         if (stats) {
             unsigned long long sl = st_leaves, sn = st_nodes, sc = st_cands, q = valid ? 1ull : 0ull;

@@ -413,6 +413,7 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         c.cnns_warp = cfg->search_mode == 2;
         c.use_graph = cfg->host_rounds == 0;
         if (cfg->search_shape > 0) c.search_shape = cfg->search_shape - 1;
+        if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);
@@ -516,7 +517,7 @@ const char* emst_last_error(const emst_ctx* x) { return x ? x->c.err.c_str() : "
 emst_status emst_set_stream(emst_ctx* x, void* stream)
 {
     if (!x) return EMST_EINVAL;
-    x->c.stream = stream ? (cudaStream_t)stream : x->c.own_stream;
+    x->c.stream = stream == EMST_OWN_STREAM ? x->c.own_stream : (cudaStream_t)stream;  // NULL: legacy default
     return EMST_OK;
 }
 

@@ -21,6 +21,7 @@
 //   act/roots/prov/zero     work lists (leaf positions)
 //   edges     2(n-1) int32  output edges (input ids, u < v); eround: round per edge
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -141,6 +142,11 @@ struct Ctx {
     // learned proposal (proposal.cuh): packed weights, radius margin (log2)
     bool learned = false;
     float margin = 1.f;
+    // plain first pass: a point whose lower bound exceeds this factor times
+    // its component's smallest waits for the second pass.  Default: none waits
+    // (one pass); with the query lists compacted before each pass, deferring
+    // measured slower on GB300 for every factor tried (1.0001 .. 16)
+    float first_pass_factor = INFINITY;
     float threshold = 0.f;
     DevBuf<unsigned char> pfrag;
     // search traces for training: records of prop::kRec floats, 1 in 2^shift

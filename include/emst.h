@@ -58,7 +58,13 @@ typedef struct {
     int search_shape;      /* component search launch shape: 0 = default for
                               the dimension, k = entry k-1 of the shape table
                               (emst_search_shape_info); see emst_autotune */
-    int reserved[4];
+    float first_pass_factor; /* component search, first pass: a point whose
+                              lower bound of d2 exceeds this factor times the
+                              smallest in its component waits for the second
+                              pass (searched only if the component's key does
+                              not rule it out); 0 = default; INFINITY = one
+                              pass */
+    int reserved[3];
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel
@@ -99,7 +105,11 @@ emst_status emst_destroy(emst_ctx* ctx);
 const char* emst_last_error(const emst_ctx* ctx);
 
 /* Bind the context's work to an existing CUDA stream (cudaStream_t passed as
- * a void*); NULL restores the context's own stream. */
+ * a void*).  NULL is the legacy default stream, as everywhere in CUDA: work
+ * the caller queued there before the call runs first, and device outputs are
+ * ready for work the caller queues there afterwards.  EMST_OWN_STREAM returns
+ * to the context's own (non-blocking) stream, where a new context starts. */
+#define EMST_OWN_STREAM ((void*)(intptr_t)-1)
 emst_status emst_set_stream(emst_ctx* ctx, void* stream);
 
 /* ---------------------------------------------------------------------------

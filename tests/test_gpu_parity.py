@@ -268,6 +268,35 @@ def test_autotune_rejects_static_mode(gpu_lib):
             e.autotune(family("uniform", 1000, 2, 44))
 
 
+@pytest.mark.parametrize("which", ["default", "side"])
+def test_device_outputs_ordered_on_caller_stream(gpu_lib, which):
+    """Device outputs are ready for work the caller queues next on the stream
+    it bound (the legacy default stream, or a stream of its own), with no
+    extra synchronisation -- also right after another context freed its
+    buffers, whose stale contents must never show through."""
+    torch = pytest.importorskip("torch")
+    pts = family("cluster", 60000, 3, 91)
+    n = len(pts)
+    with gpu_lib.Emst() as e:
+        ref, ref_len = e.solve(pts)
+    ref = _canon(ref)
+    stream = torch.cuda.Stream() if which == "side" else torch.cuda.default_stream()
+    with torch.cuda.stream(stream):
+        dev = torch.from_numpy(pts).cuda()
+        uv = torch.full((n - 1, 2), -1, dtype=torch.int32, device="cuda")
+        ln = torch.zeros(1, dtype=torch.float64, device="cuda")
+        for rep in range(6):
+            with gpu_lib.Emst() as e:
+                e.set_stream(stream.cuda_stream)
+                uv.fill_(-1)
+                e.solve_device(dev.data_ptr(), n, 3, uv.data_ptr(), ln.data_ptr())
+                got = uv.cpu().numpy()  # queued on the same stream: must see the solve's output
+                assert np.array_equal(_canon(got), ref), rep
+                assert ln.item() == pytest.approx(ref_len, rel=1e-12)
+            with gpu_lib.Emst(host_rounds=True) as e2:  # frees buffers between the timed contexts
+                e2.solve(pts)
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
