@@ -17,6 +17,7 @@ OpenMP over all host cores), each step a bounded sample of the same workload.
 Under torchrun (N > 1) every rank solves its own replica ("replicas only").
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -31,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "component-based-2d-3d-nns-to-gpu-parallel-2d-3d-emst_gb300")
 sys.path.insert(0, PKG)
 
-METRIC = "EMST Mpoints/s at 1e7 pts (plain Boruvka, exact edge set); % HBM roofline"
+METRIC = "EMST Mpoints/s at 1e7 pts (learned vs plain, same edge set); % HBM roofline"
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -162,6 +163,67 @@ def batch_bench(E, device, reps=3):
             "note": "wall clock, host points in / host edges + lengths out, same edge sets"}
 
 
+def edge_hash(d_uv):
+    """Canonical hash of an edge list on the device: pairs (min, max), sorted."""
+    a = np.sort(d_uv.cpu().numpy().astype(np.int64), axis=1)
+    key = np.sort(a[:, 0] * (1 << 32) + a[:, 1])
+    return hashlib.sha1(key.tobytes()).hexdigest()
+
+
+def learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, dim, plain_ms):
+    """Learned-vs-plain comparison on the benchmark workload: device time of the
+    same steps, edge-set identity, and the proposal's counters."""
+    import torch
+    import emst_proposal as PR
+    w, info = PR.load()
+    if w is None:
+        return {"unavailable": "no trained weights (run emst_proposal.py)"}
+    plain_hash = edge_hash(d_uv)
+    margin = float(info.get("margin", PR.DEFAULT_MARGIN))
+    thr = float(info.get("threshold", PR.DEFAULT_THRESHOLD))
+    ms = []
+    with E.Emst(device=local, search_shape=shape) as lc:
+        lc.set_stream(stream.cuda_stream)
+        lc.set_proposal(w, margin, thr)
+        for _ in range(args.warmup):
+            lc.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            lc.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    same = edge_hash(d_uv) == plain_hash
+
+    def counters(weights):
+        with E.Emst(device=local, profile=True, search_shape=shape) as pc:
+            pc.set_stream(stream.cuda_stream)
+            if weights is not None:
+                pc.set_proposal(weights, margin, thr)
+            pc.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+            return pc.profile()
+
+    pp, pl = counters(None), counters(w)
+    K = len(ms)
+
+    def per(p):
+        q = max(p["search_queries"], 1)
+        return {"searches_per_point": p["search_queries"] / n, "cells_visited_per_query": p["leaf_visits"] / q,
+                "cells_visited_per_point": p["leaf_visits"] / n, "node_tests_per_query": p["node_tests"] / q,
+                "first_pass_searches": p["first_pass_searches"], "deferred": p["first_pass_deferred"]}
+    return {"value": n * K / (sum(ms) / 1e3) / 1e6, "unit": "Mpoints/s", "ms_per_step": sum(ms) / K,
+            "plain_value": n * len(plain_ms) / (sum(plain_ms) / 1e3) / 1e6, "vs_plain": sum(plain_ms) / len(plain_ms) / (sum(ms) / K),
+            "same_edge_set": same, "margin": margin, "threshold": thr,
+            "mispredict_rate": pl["first_pass_resumed"] / max(pl["first_pass_searches"], 1),
+            "plain": per(pp), "learned": per(pl),
+            "weights": {k: info.get(k) for k in ("records", "clouds", "points_per_cloud", "generator", "epochs",
+                                                  "loss_curve")},
+            "note": "value is the learned form; the top-level value is the plain form (the library default)"}
+
+
 def run_reference(args, pts, dim):
     """The CPU restatement of the reference's path, all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -203,6 +265,7 @@ def main():
     ap.add_argument("--no-static", action="store_true", help="skip the one-step static-table comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-cloud batch comparison")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal leg")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -293,6 +356,12 @@ def main():
         total_ms = float(t.item())
     value = world * n * args.steps / (total_ms / 1e3) / 1e6
 
+    # learned proposal: the same steps with the trained network steering the
+    # first search pass; its edge set must equal the plain one
+    learned = None
+    if args.mode == 0 and not args.no_learned and rank == 0:
+        learned = learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, dim, dev_ms)
+
     # profiled run(s): phase split, search counters and the dominant kernel's time
     for _ in range(args.steps):
         flush.zero_()
@@ -378,7 +447,7 @@ def main():
                              "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                              "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
                              "peak_kind": peak_kind},
-                "phase_ms": phase_ms, "static_table_mode": static, "batch512": batch,
+                "phase_ms": phase_ms, "learned": learned, "static_table_mode": static, "batch512": batch,
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
                         "d2h_bytes_per_step": int(8 * (n - 1) + 8)},

@@ -361,6 +361,18 @@ struct FlagIsOne {
     __host__ __device__ bool operator()(uint32_t i) const { return f[i] == 1; }
 };
 
+struct FlagIsTwo {
+    const unsigned char* f;
+    __host__ __device__ bool operator()(uint32_t i) const { return f[i] == 2; }
+};
+
+cudaError_t select_flagged_two(Ctx& c, uint32_t* out, uint32_t* count)
+{
+    size_t tb = c.sel_tmp.cap;
+    return cub::DeviceSelect::If(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), out, count, (int)c.n,
+                                 FlagIsTwo{c.dflag.p}, c.stream);
+}
+
 cudaError_t select_flagged_one(Ctx& c, uint32_t* out, uint32_t* count)
 {
     size_t tb = c.sel_tmp.cap;
@@ -462,6 +474,8 @@ cudaError_t cnns_select(Ctx& c)
                                                               c.clb.p, first_factor, st);
         c.launches++;
         e = select_flagged_one(c, c.dirty.p, &d->n_dirty);
+        if (e == cudaSuccess && c.first_pass_ordered && !(c.learned && !c.n_clouds))
+            e = select_flagged_two(c, c.dirty2.p, &d->n_dirty2);
     }
     if (e != cudaSuccess) return e;
     constexpr int WPB = 4;
@@ -486,7 +500,13 @@ cudaError_t cnns_select(Ctx& c)
             CnnsArgs a{c.spl.p,  c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
                        cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
                        c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
-                       c.threshold, &d->round};
+                       c.threshold, &d->round,   nullptr,  nullptr};
+            const bool ordered = c.first_pass_ordered && !(c.learned && !pc);
+            if (ordered) {  // both segments in this one launch; no second pass
+                if (pass == 2) continue;
+                a.list2 = c.dirty2.p;
+                a.n_list2 = &d->n_dirty2;
+            }
             const int shape = search_shape_of(c);
             const bool learned = c.learned && pass == 1 && !pc;
             if (pass == 1 && c.trace_cap > 0 && !learned) {
@@ -496,7 +516,7 @@ cudaError_t cnns_select(Ctx& c)
             cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
-            if (pass == 1) {
+            if (pass == 1 && !ordered) {
                 k_filter_second<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p,
                                                                              c.lbp.p, c.ckey.p);
                 c.launches++;

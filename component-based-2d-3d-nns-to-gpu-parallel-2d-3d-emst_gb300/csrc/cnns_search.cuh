@@ -69,11 +69,13 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     // kernel uses no shared memory, so the SM keeps its whole L1 for the search
     const prop::Frag* W = reinterpret_cast<const prop::Frag*>(a.frag);
     const int round = LEARN ? *a.round : 0;
-    const uint32_t total = *n_list;
+    // the queries: list, then (one launch, second segment) list2
+    const uint32_t n1 = *n_list;
+    const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
     for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
         const uint32_t qi = base0 + threadIdx.x;
         const bool listed = qi < total;
-        const uint32_t me = listed ? list[qi] : 0u;
+        const uint32_t me = listed ? (qi < n1 ? list[qi] : a.list2[qi - n1]) : 0u;
         const uint32_t labp = listed ? lab[me] : kEmpty;
         const float lb0 = listed ? lbp[me] : 0.f;
         bool valid = listed, deferred = false;

@@ -414,6 +414,7 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         c.use_graph = cfg->host_rounds == 0;
         if (cfg->search_shape > 0) c.search_shape = cfg->search_shape - 1;
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
+        c.first_pass_ordered = cfg->first_pass_ordered != 0;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);

@@ -147,6 +147,9 @@ struct Ctx {
     // (one pass); with the query lists compacted before each pass, deferring
     // measured slower on GB300 for every factor tried (1.0001 .. 16)
     float first_pass_factor = INFINITY;
+    // one search launch per round: the points the factor keeps first, the
+    // others after them (instead of a second pass)
+    bool first_pass_ordered = false;
     float threshold = 0.f;
     DevBuf<unsigned char> pfrag;
     // search traces for training: records of prop::kRec floats, 1 in 2^shift
@@ -218,6 +221,8 @@ struct CnnsArgs {
     float margin;      // learned proposal: log2 margin added to the predicted radius
     float threshold;   // learned proposal: class logit at or above which a point searches first
     const int* round;  // rounds started (device)
+    const uint32_t* list2;    // second segment of the same launch (ordered first pass), or null
+    const uint32_t* n_list2;
 };
 
 // Launch shapes of the component search: threads per block and the minimum

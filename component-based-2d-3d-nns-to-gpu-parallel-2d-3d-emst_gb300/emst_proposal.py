@@ -26,7 +26,8 @@ import emst_workloads as W
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 WEIGHTS_PATH = os.path.join(HERE, "proposal_weights.json")
-DEFAULT_MARGIN = 1.0
+DEFAULT_MARGIN = 4.0     # log2 factor on the predicted radius (d2)
+DEFAULT_THRESHOLD = 1.0  # class logit at or above which a point searches first
 
 
 def training_clouds(n_clouds=64, n=1_000_000, first_seed=1000, clusters=256):
@@ -55,7 +56,7 @@ def fit(n_clouds=64, n=1_000_000, sample_shift=4, epochs=4, batch=4096, lr=2e-3,
             "generator": "gauss_mixture(n, 3, 256 clusters, seed), seeds %d..%d" % (1000, 1000 + n_clouds - 1),
             "epochs": epochs, "batch": batch, "lr": lr, "reg_weight": reg_weight, "seed": seed,
             "loss_curve": [float(v) for v in curve], "trace_s": t1 - t0, "train_s": t2 - t1,
-            "margin": DEFAULT_MARGIN}
+            "margin": DEFAULT_MARGIN, "threshold": DEFAULT_THRESHOLD}
     return w, info
 
 

@@ -64,7 +64,10 @@ typedef struct {
                               pass (searched only if the component's key does
                               not rule it out); 0 = default; INFINITY = one
                               pass */
-    int reserved[3];
+    int first_pass_ordered; /* != 0: one search launch per round, the points
+                              the factor keeps first and the others after
+                              them, instead of a second pass */
+    int reserved[2];
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel

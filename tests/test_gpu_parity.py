@@ -297,6 +297,24 @@ def test_device_outputs_ordered_on_caller_stream(gpu_lib, which):
                 e2.solve(pts)
 
 
+@pytest.mark.parametrize("kw", [dict(first_pass_factor=1.0001), dict(first_pass_factor=4.0),
+                                dict(first_pass_factor=1.5, first_pass_ordered=True),
+                                dict(first_pass_factor=float("inf"), first_pass_ordered=True)])
+@pytest.mark.parametrize("kind,dim", [("cluster", 3), ("dups", 2), ("lattice", 3)])
+def test_first_pass_rules_keep_edges(gpu_lib, kw, kind, dim):
+    """The first-pass rule (who searches first, in one launch or two) only
+    changes the order of the searches, never the edge set."""
+    pts = family(kind, 20000, dim, 71)
+    with gpu_lib.Emst() as e:
+        ref, ref_len = e.solve(pts)
+        ref_rounds = e.round_stats()
+    with gpu_lib.Emst(**kw) as e:
+        uv, ln = e.solve(pts)
+        assert np.array_equal(_canon(uv), _canon(ref))
+        assert ln == pytest.approx(ref_len, rel=1e-12)
+        assert np.array_equal(e.round_stats(), ref_rounds)
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
