@@ -690,6 +690,16 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     return EMST_OK;
 }
 
+emst_status emst_get_size(emst_ctx* x, int64_t* n, int* dim)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    if (x->c.n_clouds) return set_err(x, EMST_EINVAL, "the context holds a batch of clouds");
+    if (n) *n = x->c.n;
+    if (dim) *dim = x->c.dim;
+    return EMST_OK;
+}
+
 emst_status emst_get_rescaled(emst_ctx* x, float* out, double* unit_x, int64_t cap)
 {
     emst_status st = check_ready(x);

@@ -94,6 +94,8 @@ def lib():
             "emst_get_trace": [P, P, i64, P], "emst_get_trace_device": [P, P, P],
             "emst_proposal_init": [ctypes.c_uint64, P], "emst_proposal_train": [P, i64, I, P, P, P],
             "emst_proposal_grad": [P, P, i64, ctypes.c_float, P, P],
+            "emst_read_points": [ctypes.c_char_p, P, i64, P, P], "emst_write_results": [P, ctypes.c_char_p],
+            "emst_read_links": [ctypes.c_char_p, P, i64, P, P], "emst_get_size": [P, P, P],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -113,6 +115,33 @@ def search_shapes():
     m = np.zeros(cnt.value, np.int32)
     lib().emst_search_shape_info(ctypes.byref(cnt), _p(t), _p(m), cnt.value)
     return cnt.value, t, m
+
+
+def read_points(path):
+    """A point file of the reference's formats -> (n, dim) float32."""
+    n, d = ctypes.c_int64(), ctypes.c_int()
+    st = lib().emst_read_points(str(path).encode(), None, 0, ctypes.byref(n), ctypes.byref(d))
+    if st != 0:
+        raise EmstError(st, "cannot read points from %s" % path)
+    out = np.zeros((n.value, d.value), np.float32)
+    if n.value:
+        st = lib().emst_read_points(str(path).encode(), _p(out), n.value, ctypes.byref(n), ctypes.byref(d))
+        if st != 0:
+            raise EmstError(st, "cannot read points from %s" % path)
+    return out
+
+
+def read_links(path):
+    """A .links file -> ((m, 2) int32 edges u < v, number of points)."""
+    m, npts = ctypes.c_int64(), ctypes.c_int64()
+    st = lib().emst_read_links(str(path).encode(), None, 0, ctypes.byref(m), ctypes.byref(npts))
+    if st != 0:
+        raise EmstError(st, "cannot read links from %s" % path)
+    uv = np.zeros((max(m.value, 1), 2), np.int32)
+    st = lib().emst_read_links(str(path).encode(), _p(uv), m.value, ctypes.byref(m), ctypes.byref(npts))
+    if st != 0:
+        raise EmstError(st, "cannot read links from %s" % path)
+    return uv[: m.value], npts.value
 
 
 def proposal_init(seed=0):
@@ -360,6 +389,10 @@ class Emst:
         ptr, cnt = ctypes.c_void_p(), ctypes.c_int64()
         self._chk(lib().emst_get_trace_device(self.h, ctypes.byref(ptr), ctypes.byref(cnt)))
         return ptr.value, cnt.value
+
+    def write_results(self, base):
+        """<base>.links, <base>.disjointSetMap, <base>.points of the finished solve."""
+        self._chk(lib().emst_write_results(self.h, str(base).encode()))
 
     def solve_device(self, d_points, n, dim, d_uv, d_length):
         ne = ctypes.c_int64()

@@ -199,6 +199,8 @@ emst_status emst_get_profile(emst_ctx* ctx, emst_profile* out);
 /* Rescaled coordinates (n * dim floats, input order) and unitX
  * (SolutionEMST.cu:305-364). */
 emst_status emst_get_rescaled(emst_ctx* ctx, float* out, double* unit_x, int64_t cap);
+/* Point count and dimension of the context's (single-cloud) point set. */
+emst_status emst_get_size(emst_ctx* ctx, int64_t* n, int* dim);
 
 /* ---------------------------------------------------------------------------
  * One-shot solvers
@@ -225,6 +227,31 @@ emst_status emst_solve_batch(emst_ctx* ctx, const float* points, const int64_t* 
  * termination read. */
 emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
                               double* d_length, int64_t* n_edges);
+
+/* ---------------------------------------------------------------------------
+ * The reference's files (host code; no GPU work)
+ * ------------------------------------------------------------------------- */
+
+/* Reads a point file the way InputRW::readFile does
+ * (emst_coalition/include/InputRW.h:60-623): the suffix picks the format --
+ * ".2d" (count, then x y per point), ".3d" (count, then x y z), ".points"
+ * ("Width = W Height = H", then x y z per point), anything else TSPLIB
+ * (DIMENSION, then "i x y" lines after NODE_COORD_SECTION).  Call with
+ * points NULL for *n and *dim, then with cap >= *n points (n * dim floats). */
+emst_status emst_read_points(const char* path, float* points, int64_t cap, int64_t* n, int* dim);
+
+/* Writes <base>.links (per point: NumLinks and its tree neighbours as "j 0"),
+ * <base>.disjointSetMap (final root of each point as a byte offset, 4 x id)
+ * and <base>.points (rescaled coordinates, 6 significant digits), as
+ * NeuralNetEMST::writeLinks and the grid writers do
+ * (emst_coalition/include/NeuralNetEMST.h:275-326, BufferLink.h:266-279).
+ * Neighbours are listed by round, then id.  The context must hold a finished
+ * single-cloud solve. */
+emst_status emst_write_results(emst_ctx* ctx, const char* base);
+
+/* Reads a .links file into an edge list (each undirected edge once, u < v);
+ * uv NULL returns the counts only. */
+emst_status emst_read_links(const char* path, int32_t* uv, int64_t cap, int64_t* n_edges, int64_t* n_points);
 
 /* ---------------------------------------------------------------------------
  * Learned search proposal (no counterpart in the reference; it stands beside

@@ -10,8 +10,12 @@ labels (test_2D_2/outypu.disjointSetMap) and the per-round traces
 its runs recorded (test_2D_2/output, test_3D_2/output: iteration, edges so
 far, tree length).  It writes compact binary / JSON fixtures so that the
 tests never need the reference checkout.  No TSPLIB instance is copied.
+For the file-format tests it also keeps the raw bytes of the two 1000-point
+input files (1000randomCity.2d / .3d) and the SHA-256 and size of the golden
+outypu.points / outypu.disjointSetMap files (reference_files.json).
 """
 import ctypes
+import hashlib
 import json
 import os
 import re
@@ -105,6 +109,14 @@ def main(ref):
     # disjointSetMap holds byte offsets of 4-byte labels (GridOfNodes.h:454-464)
     dsm = open(os.path.join(t2, "outypu.disjointSetMap")).read().split()[6:]
     arrays["outypu_labels"] = (np.array([int(v) for v in dsm], dtype=np.int64) // 4).astype(np.int32)
+    arrays["raw_2d_1000"] = np.frombuffer(open(os.path.join(t2, "1000randomCity.2d"), "rb").read(), np.uint8)
+    arrays["raw_3d_1000"] = np.frombuffer(open(os.path.join(t3, "1000randomCity.3d"), "rb").read(), np.uint8)
+    files = {}
+    for name in ("outypu.points", "outypu.disjointSetMap"):
+        data = open(os.path.join(t2, name), "rb").read()
+        files[name] = {"sha256": hashlib.sha256(data).hexdigest(), "bytes": len(data)}
+    with open(os.path.join(HERE, "reference_files.json"), "w") as fo:
+        json.dump(files, fo, indent=1)
     np.savez_compressed(os.path.join(HERE, "reference_fixtures.npz"), **arrays)
     traces = {"2d": read_traces(os.path.join(t2, "output")), "3d": read_traces(os.path.join(t3, "output"))}
     with open(os.path.join(HERE, "reference_traces.json"), "w") as fo:

@@ -1,0 +1,77 @@
+"""Result files on the GPU path: the golden 3000-point set written the way the
+reference writes it, compared with the reference's own files, and the
+command-line driver end to end."""
+import hashlib
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import emst_gb300 as E
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _canon(uv):
+    a = np.sort(np.asarray(uv, np.int64), axis=1)
+    return a[np.lexsort((a[:, 1], a[:, 0]))]
+
+
+def _sha(path):
+    return hashlib.sha256(open(path, "rb").read()).hexdigest()
+
+
+def test_results_match_reference_files(gpu_lib, fixtures, tmp_path):
+    ref = json.load(open(os.path.join(GOLDEN, "reference_files.json")))
+    pts = fixtures["pts2d_3000"]
+    base = str(tmp_path / "outypu")
+    with gpu_lib.Emst() as e:
+        e.solve(pts)
+        e.write_results(base)
+    uv, npts = gpu_lib.read_links(base + ".links")
+    assert npts == 3000
+    assert np.array_equal(_canon(uv), _canon(fixtures["outypu_edges"]))
+    # final roots as byte offsets: the reference's file, byte for byte
+    assert _sha(base + ".disjointSetMap") == ref["outypu.disjointSetMap"]["sha256"]
+    # rescaled coordinates at 6 significant digits
+    toks = open(base + ".points").read().split()
+    assert toks[:6] == ["Width", "=", "3000", "Height", "=", "1"]
+    got = np.array([float(t) for t in toks[6:]]).reshape(3000, 3)
+    assert np.allclose(got[:, :2], fixtures["outypu_points"], rtol=1e-5, atol=1e-4) and np.all(got[:, 2] == 0)
+    # every point has a record; degrees sum to 2 (n - 1)
+    txt = open(base + ".links").read()
+    assert txt.count("NodeP =") == 3000
+
+
+def test_points_file_bytes(gpu_lib, fixtures, tmp_path):
+    """The .points file reproduces the reference's byte for byte when every
+    rescaled float prints the same at 6 significant digits."""
+    ref = json.load(open(os.path.join(GOLDEN, "reference_files.json")))
+    base = str(tmp_path / "outypu")
+    with gpu_lib.Emst() as e:
+        e.solve(fixtures["pts2d_3000"])
+        e.write_results(base)
+    data = open(base + ".points", "rb").read()
+    assert len(data) == ref["outypu.points"]["bytes"]
+    assert hashlib.sha256(data).hexdigest() == ref["outypu.points"]["sha256"]
+
+
+def test_cli_end_to_end(gpu_lib, fixtures, tmp_path):
+    exe = os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "emst_run")
+    assert os.path.exists(exe), "emst_run is built with the library"
+    data = tmp_path / "1000randomCity.2d"
+    data.write_bytes(bytes(fixtures["raw_2d_1000"]))
+    sol, stats = tmp_path / "run1.svg", tmp_path / "run1.stats"
+    r = subprocess.run([exe, str(data), str(sol), str(stats)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    uv, npts = gpu_lib.read_links(str(tmp_path / "run1.links"))
+    with gpu_lib.Emst() as e:
+        ref, length = e.solve(fixtures["pts2d_1000"])
+    assert npts == 1000 and np.array_equal(_canon(uv), _canon(ref))
+    f = open(stats).read().split()
+    assert int(f[0]) == 1000 and int(f[1]) == 2 and int(f[2]) == 999
+    assert float(f[3]) == pytest.approx(length, rel=1e-6)
+    assert os.path.exists(tmp_path / "run1.disjointSetMap") and os.path.exists(tmp_path / "run1.points")
