@@ -452,9 +452,29 @@ cudaError_t evaluate_length(Ctx& c, double* d_out)
     return cudaGetLastError();
 }
 
-cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out)
+cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out, const uint32_t* src)
 {
-    k_labels_out<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.perm.p, d_out);
+    k_labels_out<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, src ? src : c.lab.p, c.perm.p, d_out);
+    c.launches++;
+    return cudaGetLastError();
+}
+
+// Labels after the round that just ended (rounds 1..cap), for the per-round
+// forests (EMSF): snapshot r-1 holds the flattened roots after round r.
+__global__ void k_snapshot(uint32_t n, const uint32_t* __restrict__ lab, const DevCounters* dc, uint32_t cap,
+                           uint32_t* __restrict__ snaps)
+{
+    const int r = dc->round;
+    if (r < 1 || (uint32_t)r > cap) return;
+    uint32_t* out = snaps + (size_t)(r - 1) * n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = lab[i];
+}
+
+cudaError_t snapshot_labels(Ctx& c)
+{
+    if (!c.snap_cap) return cudaSuccess;
+    const unsigned b = (unsigned)std::min<int64_t>(blocks_for(c.n, 256), (int64_t)c.sms * 8);
+    k_snapshot<<<b ? b : 1, 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.ctr.p, (uint32_t)c.snap_cap, c.snaps.p);
     c.launches++;
     return cudaGetLastError();
 }

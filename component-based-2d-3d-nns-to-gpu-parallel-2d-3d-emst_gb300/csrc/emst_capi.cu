@@ -138,6 +138,7 @@ emst_status do_flatten(emst_ctx* x)
     if (c.round > 0) {
         Timed t(x, PH_FLATTEN);
         EMST_CUDA(x, emst::boruvka_flatten(c), "flatten");
+        EMST_CUDA(x, emst::snapshot_labels(c), "snapshot");
     }
     emst_status st = read_counters(x);
     if (st != EMST_OK) return st;
@@ -257,6 +258,11 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
         EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
         EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), c.stream), "stats");
     }
+    c.snap_cap = 0;
+    if (c.snap_rounds > 0) {
+        EMST_CUDA(x, emst::ensure(c.snaps, (size_t)c.snap_rounds * n), "alloc snapshots");
+        c.snap_cap = c.snap_rounds;
+    }
     for (double& v : x->ms) v = 0.0;
     {
         Timed t(x, PH_GRID);
@@ -294,6 +300,7 @@ emst_status enqueue_round(emst_ctx* x, cudaGraphConditionalHandle h)
     EMST_CUDA(x, emst::boruvka_resolve(c), "find_min_pair");
     EMST_CUDA(x, emst::boruvka_hook(c), "connect_union");
     EMST_CUDA(x, emst::boruvka_flatten(c), "flatten");
+    EMST_CUDA(x, emst::snapshot_labels(c), "snapshot");
     EMST_CUDA(x, emst::round_end(c, h), "round end");
     return EMST_OK;
 }
@@ -311,7 +318,8 @@ emst_status build_graph(emst_ctx* x)
                                     (const void*)(intptr_t)emst::search_shape_of(c), c.pfrag.p,
                                     (const void*)(intptr_t)(c.learned ? 1 : 0), c.trace.p,
                                     (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
-                                    (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p};
+                                    (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p, c.snaps.p,
+                                    (const void*)(intptr_t)c.snap_cap};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
     cudaGraph_t g = nullptr, body = nullptr;
@@ -460,6 +468,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.pfrag);
     emst::release(c.trace);
     emst::release(c.trace_ctl);
+    emst::release(c.snaps);
     emst::release(c.sel_tmp);
     emst::release(c.lbp);
     emst::release(c.clb);
@@ -690,6 +699,30 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     return EMST_OK;
 }
 
+emst_status emst_keep_round_labels(emst_ctx* x, int rounds)
+{
+    if (!x || rounds < 0 || rounds > 100) return EMST_EINVAL;
+    x->c.snap_rounds = rounds;  // takes effect from the next initialize / solve
+    return EMST_OK;
+}
+
+emst_status emst_get_round_labels(emst_ctx* x, int round, int32_t* labels, int64_t cap)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (c.n_clouds) return set_err(x, EMST_EINVAL, "the context holds a batch of clouds");
+    if (round < 1 || round > (int)c.cum_edges.size()) return set_err(x, EMST_EINVAL, "no such round");
+    if (round > c.snap_cap) return set_err(x, EMST_EINVAL, "round labels not kept (emst_keep_round_labels)");
+    if (!labels || cap < c.n) return set_err(x, EMST_EOVERFLOW, "labels buffer too small");
+    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)c.n), "alloc");
+    EMST_CUDA(x, emst::labels_to_input_order(c, x->tmp_i32.p, c.snaps.p + (size_t)(round - 1) * c.n), "labels");
+    EMST_CUDA(x, cudaMemcpyAsync(labels, x->tmp_i32.p, sizeof(int32_t) * c.n, cudaMemcpyDeviceToHost, c.stream),
+              "labels");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "labels");
+    return EMST_OK;
+}
+
 emst_status emst_get_size(emst_ctx* x, int64_t* n, int* dim)
 {
     emst_status st = check_ready(x);
@@ -780,6 +813,7 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
     EMST_CUDA(x, cudaMemcpyAsync(c.d_dims.p, dims, sizeof(int32_t) * n_clouds, cudaMemcpyHostToDevice, s), "upload");
     c.in = c.in_own.p;
     c.n = n;
+    c.snap_cap = 0;  // per-round labels are kept for single-cloud solves only
     c.dim = 3;  // 2D clouds carry z = 0 (fma(0, 0, r) == r keeps their distances 2D)
     c.K = 24;
     c.n_clouds = n_clouds;

@@ -158,6 +158,10 @@ struct Ctx {
     int64_t trace_cap = 0;
     int trace_shift = 0;
     DevBuf<uint32_t> trace_ctl;
+    // per-round labels (EMSF snapshots): rounds kept, buffer of snap_cap * n roots
+    int snap_rounds = 0;
+    int64_t snap_cap = 0;
+    DevBuf<uint32_t> snaps;
 
     int round = 0;        // rounds started
     int phase = 0;        // 0 = not initialised, 1 = initialised
@@ -186,7 +190,8 @@ cudaError_t boruvka_count_other(Ctx& c);
 cudaError_t round_tick(Ctx& c);
 cudaError_t round_end(Ctx& c, cudaGraphConditionalHandle h);
 cudaError_t evaluate_length(Ctx& c, double* d_out);
-cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out);
+cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out, const uint32_t* src = nullptr);
+cudaError_t snapshot_labels(Ctx& c);
 cudaError_t table_to_host_order(Ctx& c);
 // cnns.cu
 cudaError_t cnns_init(Ctx& c);

@@ -96,6 +96,7 @@ def lib():
             "emst_proposal_grad": [P, P, i64, ctypes.c_float, P, P],
             "emst_read_points": [ctypes.c_char_p, P, i64, P, P], "emst_write_results": [P, ctypes.c_char_p],
             "emst_read_links": [ctypes.c_char_p, P, i64, P, P], "emst_get_size": [P, P, P],
+            "emst_keep_round_labels": [P, I], "emst_get_round_labels": [P, I, P, i64],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -389,6 +390,16 @@ class Emst:
         ptr, cnt = ctypes.c_void_p(), ctypes.c_int64()
         self._chk(lib().emst_get_trace_device(self.h, ctypes.byref(ptr), ctypes.byref(cnt)))
         return ptr.value, cnt.value
+
+    def keep_round_labels(self, rounds):
+        """Keep each point's root after each of the first `rounds` rounds (next solve on)."""
+        self._chk(lib().emst_keep_round_labels(self.h, int(rounds)))
+
+    def round_labels(self, r):
+        """Roots (input ids) after round r of the last solve."""
+        out = np.zeros(self.n, np.int32)
+        self._chk(lib().emst_get_round_labels(self.h, int(r), _p(out), self.n))
+        return out
 
     def write_results(self, base):
         """<base>.links, <base>.disjointSetMap, <base>.points of the finished solve."""

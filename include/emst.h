@@ -199,6 +199,15 @@ emst_status emst_get_profile(emst_ctx* ctx, emst_profile* out);
 /* Rescaled coordinates (n * dim floats, input order) and unitX
  * (SolutionEMST.cu:305-364). */
 emst_status emst_get_rescaled(emst_ctx* ctx, float* out, double* unit_x, int64_t cap);
+/* Hierarchical EMSF (the reference reads the forest back after every round,
+ * SolutionEMSTOperators.cu:145-153, 413-416): the forest after round k is
+ * the edges whose round_of_edge (emst_get_edges) is <= k.  To also get each
+ * point's union-find root after round k, ask the context to keep the labels
+ * of the first `rounds` rounds (n * rounds * 4 bytes of device memory) before
+ * solving; emst_get_round_labels then returns them in emst_get_labels' form. */
+emst_status emst_keep_round_labels(emst_ctx* ctx, int rounds);
+emst_status emst_get_round_labels(emst_ctx* ctx, int round, int32_t* labels, int64_t cap);
+
 /* Point count and dimension of the context's (single-cloud) point set. */
 emst_status emst_get_size(emst_ctx* ctx, int64_t* n, int* dim);
 

@@ -75,3 +75,57 @@ def test_cli_end_to_end(gpu_lib, fixtures, tmp_path):
     assert int(f[0]) == 1000 and int(f[1]) == 2 and int(f[2]) == 999
     assert float(f[3]) == pytest.approx(length, rel=1e-6)
     assert os.path.exists(tmp_path / "run1.disjointSetMap") and os.path.exists(tmp_path / "run1.points")
+
+
+@pytest.mark.parametrize("host", [False, True])
+@pytest.mark.parametrize("case", ["golden2d", "cluster3d", "dups2d"])
+def test_round_forests_and_labels(gpu_lib, fixtures, case, host):
+    """Hierarchical EMSF: after every round, the kept roots are constant on each
+    tree of the forest of edges up to that round and differ between trees,
+    every root is a point of its own tree, roots only disappear, and the last
+    round's roots are the final labels (pinned to the reference's
+    disjointSetMap for the golden set)."""
+    from families import family
+    pts = {"golden2d": fixtures["pts2d_3000"], "cluster3d": family("cluster", 20000, 3, 5),
+           "dups2d": family("dups", 5000, 2, 6)}[case]
+    n = len(pts)
+    with gpu_lib.Emst(host_rounds=host) as e:
+        e.keep_round_labels(32)
+        e.solve(pts)
+        uv, rd = e.edges(with_rounds=True)
+        final = e.labels()
+        cum = e.round_stats()
+        R = len(cum)
+        snaps = [e.round_labels(r) for r in range(1, R + 1)]
+        with pytest.raises(gpu_lib.EmstError):
+            e.round_labels(R + 1)
+    if case == "golden2d":
+        assert np.array_equal(final, fixtures["outypu_labels"])
+    assert np.array_equal(snaps[-1], final)
+    prev_roots = None
+    for r in range(1, R + 1):
+        lab = snaps[r - 1]
+        sel = rd <= r
+        assert int(sel.sum()) == int(cum[r - 1])
+        # union-find over the forest up to round r
+        par = np.arange(n)
+
+        def find(a):
+            while par[a] != a:
+                par[a] = par[par[a]]
+                a = par[a]
+            return a
+        for u, v in uv[sel]:
+            ru, rv = find(u), find(v)
+            if ru != rv:
+                par[max(ru, rv)] = min(ru, rv)
+        comp = np.array([find(i) for i in range(n)])
+        # same tree <=> same label, and the label is a member of the tree
+        assert len(np.unique(comp)) == len(np.unique(lab)) == n - int(cum[r - 1])
+        pairs = np.unique(np.stack([comp, lab], 1), axis=0)
+        assert len(pairs) == len(np.unique(comp))
+        assert np.array_equal(comp[lab], comp)
+        roots = set(np.unique(lab).tolist())
+        if prev_roots is not None:
+            assert roots <= prev_roots
+        prev_roots = roots
