@@ -280,12 +280,19 @@ __global__ void k_edge_len(const int32_t* __restrict__ edges, uint32_t ne, const
     }
 }
 
-__global__ void k_sum_parts(const double* __restrict__ part, int nb, double* __restrict__ out)
+// One block sums the per-block partials in a fixed order (deterministic).
+__global__ void __launch_bounds__(1024) k_sum_parts(const double* __restrict__ part, int nb, double* __restrict__ out)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double t = 0.0;
-        for (int j = 0; j < nb; ++j) t += part[j];
-        *out = t;
+    __shared__ double s[32];
+    double t = 0.0;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) t += part[j];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? s[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(kFull, t, o);
+        if (threadIdx.x == 0) *out = t;
     }
 }
 
@@ -447,7 +454,7 @@ cudaError_t evaluate_length(Ctx& c, double* d_out)
         k_edge_len<2><<<nb, 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.in, c.lpart.p);
     else
         k_edge_len<3><<<nb, 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.in, c.lpart.p);
-    k_sum_parts<<<1, 32, 0, c.stream>>>(c.lpart.p, (int)nb, d_out);
+    k_sum_parts<<<1, 1024, 0, c.stream>>>(c.lpart.p, (int)nb, d_out);
     c.launches += 2;
     return cudaGetLastError();
 }
