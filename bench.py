@@ -123,7 +123,7 @@ def traffic_from_profile(name):
     return None
 
 
-def cpu_baseline(pts, threads, sample_n, seed=0):
+def cpu_baseline(pts, threads, sample_n, seed=0, with_edges=False):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     rng = np.random.default_rng(seed)
@@ -135,16 +135,61 @@ def cpu_baseline(pts, threads, sample_n, seed=0):
     r = O.emst(sp, "faithful")
     dt = time.perf_counter() - t0
     assert len(r.edges) == len(sub) - 1
+    if with_edges:
+        return len(sub) / dt / 1e6, dt, len(sub), sub, np.asarray(r.edges).reshape(-1, 2)
     return len(sub) / dt / 1e6, dt, len(sub)
 
 
-def batch_bench(E, device, reps=3):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
+def canon_edges(uv):
+    a = np.sort(np.asarray(uv, np.int64).reshape(-1, 2), axis=1)
+    return a[np.lexsort((a[:, 1], a[:, 0]))]
+
+
+def batch_bench(E, device, reps=3, rank=0, world=1, dist=None):
     """512-cloud workload (sizes log-uniform 1e3..1e5, half 2D half 3D, uniform
     or 8-cluster): clouds/s of one batched solve (emst_solve_batch) vs the plain
-    solver launched once per cloud (emst_solve), host buffers in and out."""
+    solver launched once per cloud (emst_solve), host buffers in and out.  With
+    several ranks the cloud list is sharded by cumulative size, each rank solves
+    its share on its GPU and rank 0 gathers every cloud's edges (emst_shard)."""
     import emst_workloads as W
     clouds = W.batch_clouds()
     total = sum(len(c) for c in clouds)
+    if world > 1:
+        import emst_shard
+        with E.Emst(device=device) as e:
+            emst_shard.solve_sharded(clouds, rank, world, e.solve_batch, dist)  # warm-up
+            dt = []
+            for _ in range(reps):
+                dist.barrier()
+                t0 = time.perf_counter()
+                uvs, _ = emst_shard.solve_sharded(clouds, rank, world, e.solve_batch, dist)
+                dt.append(time.perf_counter() - t0)
+        import torch
+        t = torch.tensor([sum(dt) / reps], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tb = float(t.item())
+        return {"clouds": len(clouds), "points": total, "ranks": world, "batched_clouds_per_s": len(clouds) / tb,
+                "batched_ms": 1e3 * tb,
+                "note": "cloud list sharded by cumulative size over the ranks, one batched solve per rank, edges "
+                        "gathered to rank 0; wall clock, max over ranks"}
     with E.Emst(device=device) as e:
         e.solve_batch(clouds)
         t0 = time.perf_counter()
@@ -244,6 +289,7 @@ def run_reference(args, pts, dim):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": args.workload, "n": len(pts), "dim": dim},
             "cpu_baseline": {"value": value, "unit": "Mpoints/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "%d random points of %s per step (CPU restatement of the reference's "
                                        "ring-search static pruning + Boruvka, OpenMP)" % (sample_n, args.workload)},
             "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -423,13 +469,17 @@ def main():
                       "note": "static-pruning region table (the reference's computeOctants), same edge set"}
 
     batch = None
-    if rank == 0 and not args.no_batch:
-        batch = batch_bench(E, local)
+    if not args.no_batch and (rank == 0 or world > 1):
+        batch = batch_bench(E, local, rank=rank, world=world, dist=dist)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, m = cpu_baseline(pts, 1, args.cpu_sample)
-        cpu = {"value": v, "unit": "Mpoints/s", "cores": 1, "kind": "port",
+        v, dt, m, sub, cedges = cpu_baseline(pts, 1, args.cpu_sample, with_edges=True)
+        with E.Emst(device=local) as ce:  # the same sample on the GPU: same edge set
+            guv, _ = ce.solve(sub)
+        cpu = {"value": v, "unit": "Mpoints/s", "cores": 1, "kind": "port", "cpu_model": cpu_model(),
+               "host_threads": os.cpu_count(),
+               "edge_set_match": bool(np.array_equal(canon_edges(guv), canon_edges(cedges))),
                "sample": "%d random points of %s (%.1f s), CPU restatement of the reference's ring-search static "
                          "pruning + Boruvka, single thread" % (m, args.workload, dt)}
 
