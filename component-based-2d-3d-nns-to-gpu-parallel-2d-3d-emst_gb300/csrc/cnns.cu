@@ -99,29 +99,63 @@ __global__ void __launch_bounds__(1024) k_node_labels_top(uint32_t top, uint32_t
 // Points whose previous partner is still outside their component re-submit
 // it; the others go to the dirty list and fold their lower bound into their
 // component's minimum bound clb.
-__global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, const uint32_t* __restrict__ selq,
-                        const uint64_t* __restrict__ selkey, const float* __restrict__ lbp,
-                        uint64_t* __restrict__ ckey, uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag,
-                        uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov)
+__global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* __restrict__ selq,
+                        uint64_t* __restrict__ selkey, float* __restrict__ lbp, uint64_t* __restrict__ ckey,
+                        uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag, uint32_t* __restrict__ prov,
+                        uint32_t* __restrict__ n_prov, const int* __restrict__ round,
+                        const uint64_t* __restrict__ kkey, const uint32_t* __restrict__ kpos,
+                        const uint32_t* __restrict__ perm)
 {
+    const bool lists = kkey && *round >= 2;  // round 1 builds them
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool is_dirty = false, record = false;
         if (p < n) {
             const uint32_t q = selq[p];
             const uint32_t lp = lab[p];
+            uint64_t key = kNoKey;
             if (q != kNone && lab[q] != lp) {
-                const uint64_t key = selkey[p];
-                if (key <= __ldcg(&ckey[lp])) {
-                    const uint64_t old = atomicMin((unsigned long long*)&ckey[lp], (unsigned long long)key);
-                    record = old >= key;
-                }
+                key = selkey[p];
             } else {
-                // lbp = +inf: no point outside the component exists (in a batch,
-                // the cloud is one component), and components only grow
-                const uint32_t lb = __float_as_uint(lbp[p]);
-                is_dirty = lb != 0x7f800000u;
-                if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
+                uint32_t lb = __float_as_uint(lbp[p]);
+                if (lists && lb != 0x7f800000u) {
+                    // the first neighbour outside the component is the exact
+                    // nearest outside point: every closer point precedes it
+                    bool full = true;
+                    for (int j = 0; j < kKnn; ++j) {
+                        const uint64_t kj = kkey[(size_t)p * kKnn + j];
+                        if (kj == kNoKey) {
+                            full = false;
+                            break;
+                        }
+                        const uint32_t qj = kpos[(size_t)p * kKnn + j];
+                        if (lab[qj] != lp) {
+                            const uint32_t mn = min(perm[p], (uint32_t)kj);
+                            key = (kj & 0xffffffff00000000ull) | mn;
+                            selq[p] = qj;
+                            selkey[p] = key;
+                            lbp[p] = __uint_as_float((uint32_t)(kj >> 32));
+                            break;
+                        }
+                        lb = max(lb, (uint32_t)(kj >> 32));  // non-negative floats order as their bits
+                    }
+                    if (key == kNoKey) {
+                        // none outside: a full list bounds the distance from below;
+                        // a short one held every other point of the cloud
+                        lb = full ? lb : 0x7f800000u;
+                        lbp[p] = __uint_as_float(lb);
+                    }
+                }
+                if (key == kNoKey) {
+                    // lbp = +inf: no point outside the component exists (in a batch,
+                    // the cloud is one component), and components only grow
+                    is_dirty = lb != 0x7f800000u;
+                    if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
+                }
+            }
+            if (key != kNoKey && key <= __ldcg(&ckey[lp])) {
+                const uint64_t old = atomicMin((unsigned long long*)&ckey[lp], (unsigned long long)key);
+                record = old >= key;
             }
         }
         if (p < n) dflag[p] = is_dirty ? 1 : 0;
@@ -437,6 +471,10 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
     if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
     if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
+    if (c.knn_seed && !c.cnns_warp) {
+        if ((e = ensure(c.kkey, n * kKnn)) != cudaSuccess) return e;
+        if ((e = ensure(c.kpos, n * kKnn)) != cudaSuccess) return e;
+    }
     size_t tb = 0, tb2 = 0;
     if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
                                         &c.ctr.p->n_dirty, (int)n, c.stream)) != cudaSuccess)
@@ -457,8 +495,10 @@ cudaError_t cnns_init(Ctx& c)
 cudaError_t cnns_select(Ctx& c)
 {
     DevCounters* d = c.ctr.p;  // n_dirty, n_dirty2, n_prov were zeroed by the round tick
+    const bool knn = c.knn_seed && !c.cnns_warp;
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
-                                                  c.clb.p, c.dflag.p, c.prov.p, &d->n_prov);
+                                                  c.clb.p, c.dflag.p, c.prov.p, &d->n_prov, &d->round,
+                                                  knn ? c.kkey.p : nullptr, c.kpos.p, c.perm.p);
     // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
     cudaError_t e;
@@ -500,7 +540,7 @@ cudaError_t cnns_select(Ctx& c)
             CnnsArgs a{c.spl.p,  c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
                        cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
                        c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
-                       c.threshold, &d->round,   nullptr,  nullptr};
+                       c.threshold, &d->round,   nullptr,  nullptr,   knn};
             const bool ordered = c.first_pass_ordered && !(c.learned && !pc);
             if (ordered) {  // both segments in this one launch; no second pass
                 if (pass == 2) continue;
@@ -512,6 +552,12 @@ cudaError_t cnns_select(Ctx& c)
             if (pass == 1 && c.trace_cap > 0 && !learned) {
                 cudaError_t et = proposal_trace_begin(c);
                 if (et != cudaSuccess) return et;
+            }
+            if (knn && pass == 1) {  // round 1 only (decided on the device)
+                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.kkey.p, c.kpos.p, c.sms, c.stream)
+                                            : launch_knn_first3(a, pc != nullptr, c.kkey.p, c.kpos.p, c.sms, c.stream);
+                if (ek != cudaSuccess) return ek;
+                c.launches++;
             }
             cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);

@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     const uint32_t* __restrict__ ncloud = a.ncloud;
     unsigned long long* __restrict__ stats = a.stats;
     constexpr int kTStack = 48;
+    if (a.knn_round1 && *a.round == 1) return;  // round 1 is k_knn_first's
     // learned proposal: weights stay in global memory (read-only cache); the
     // kernel uses no shared memory, so the SM keeps its whole L1 for the search
     const prop::Frag* W = reinterpret_cast<const prop::Frag*>(a.frag);
@@ -308,6 +309,183 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     }
 }
 
+// Round 1 with neighbour lists: each point's kKnn nearest other points (its
+// component is itself), sorted by (d2, input id) and kept for later rounds:
+// there, the first entry outside the point's component is its exact nearest
+// outside point -- every closer point is earlier in the list -- so most
+// points of rounds 2-4 need no search (k_reuse).  Entry 0 is the round-1
+// result, written like k_cnns_t's.  Runs only when the device round is 1.
+template <int D, bool CL>
+__global__ void __launch_bounds__(256, 3) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ kkey,
+                                                       uint32_t* __restrict__ kpos)
+{
+    if (*a.round != 1) return;
+    const float4* __restrict__ spl = a.spl;
+    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ nlo = a.nlo;
+    const float4* __restrict__ nhi = a.nhi;
+    const uint32_t* __restrict__ nlab = a.nlab;
+    const uint32_t n = a.n, L = a.L;
+    const uint32_t* __restrict__ pcloud = a.pcloud;
+    const uint32_t* __restrict__ ncloud = a.ncloud;
+    constexpr int K = kKnn, kTStack = 48;
+    const uint32_t total = *a.n_list;
+    for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
+        const uint32_t qi = base0 + threadIdx.x;
+        const bool listed = qi < total;
+        const uint32_t me = listed ? a.list[qi] : 0u;
+        const uint32_t labp = listed ? a.lab[me] : kEmpty;
+        bool record = false;
+        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
+        if (listed) {
+            const float4 P = spl[me];
+            const int op = (int)perm[me];
+            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
+            uint64_t kk[K];
+            uint32_t kp[K];
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                kk[j] = kNoKey;
+                kp[j] = kNone;
+            }
+            float bd = INFINITY;  // d2 of the K-th entry once the list is full
+            auto offer = [&](uint32_t pos, float d2) {
+                if (d2 > bd) return;
+                const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | __ldg(&perm[pos]);
+                if (key >= kk[K - 1]) return;
+                // sorted insert, all in registers
+#pragma unroll
+                for (int j = K - 1; j > 0; --j) {
+                    const bool sh = key < kk[j - 1];
+                    const bool put = !sh && key < kk[j];
+                    kk[j] = sh ? kk[j - 1] : (put ? key : kk[j]);
+                    kp[j] = sh ? kp[j - 1] : (put ? pos : kp[j]);
+                }
+                if (key < kk[0]) {
+                    kk[0] = key;
+                    kp[0] = pos;
+                }
+                if (kk[K - 1] != kNoKey) bd = __uint_as_float((uint32_t)(kk[K - 1] >> 32));
+            };
+            auto scan_leaf = [&](uint32_t leaf) {
+                const uint32_t b = leaf * 32;
+                if (b >= n) return;
+                const uint32_t m = min(32u, n - b);
+                ++st_leaves;
+                st_cands += m;
+                bool mixed = false;
+                if constexpr (CL) {
+                    const uint32_t r = __ldg(&ncloud[L + leaf]);
+                    mixed = (r >> 16) != (r & 0xffffu);
+                }
+                for (uint32_t j = 0; j < m; j += 4) {
+                    float4 c[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, __uint_as_float(labp));
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (__float_as_uint(c[k].w) == labp) continue;
+                        if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
+                        offer(b + j + k,
+                              d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z)));
+                    }
+                }
+            };
+            auto node_lb = [&](uint32_t node) -> float {
+                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                if (lo.x > hi.x) return INFINITY;
+                if (__ldg(&nlab[node]) == labp) return INFINITY;
+                if constexpr (CL) {
+                    const uint32_t r = __ldg(&ncloud[node]);
+                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
+                }
+                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+                return d2_of<D>(gx, gy, gz);
+            };
+            const uint32_t own = me >> 5;
+            scan_leaf(own);
+            uint32_t stack[kTStack];
+            for (uint32_t v = L + own; v > 1; v >>= 1) {
+                const uint32_t sib = v ^ 1u;
+                ++st_nodes;
+                const float ls = node_lb(sib);
+                if (!(ls < INFINITY) || ls > bd) continue;
+                int top = 0;
+                stack[top++] = sib;
+                while (top > 0) {
+                    uint32_t leaf = kNone;
+                    while (top > 0) {
+                        const uint32_t node = stack[--top];
+                        ++st_nodes;
+                        if (node >= L) {
+                            const float lb = node_lb(node);
+                            if (!(lb < INFINITY) || lb > bd) continue;
+                            leaf = node - L;
+                            break;
+                        }
+                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                        const float l0 = node_lb(c0), l1 = node_lb(c1);
+                        const bool near0 = l0 <= l1;
+                        const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
+                        const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
+                        if (top + 2 > kTStack) {  // cannot happen for trees of depth < 46
+                            top = 0;
+                            break;
+                        }
+                        if (lf < INFINITY && lf <= bd) stack[top++] = cf;
+                        if (ln < INFINITY && ln <= bd) stack[top++] = cn;
+                    }
+                    if (leaf != kNone) scan_leaf(leaf);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                kkey[(size_t)me * K + j] = kk[j];
+                kpos[(size_t)me * K + j] = kp[j];
+            }
+            // round-1 result: entry 0 (exact: every node within the K-th
+            // distance was searched)
+            if (kk[0] != kNoKey) {
+                const float d0 = __uint_as_float((uint32_t)(kk[0] >> 32));
+                const uint32_t mn = (uint32_t)min(op, (int)(uint32_t)kk[0]);
+                const uint64_t key = ((uint64_t)__float_as_uint(d0) << 32) | mn;
+                a.lbp[me] = d0;
+                a.selq[me] = kp[0];
+                a.selkey[me] = key;
+                if (key <= __ldcg(&a.ckey[labp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&a.ckey[labp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                a.lbp[me] = INFINITY;  // alone in its cloud
+                a.selq[me] = kNone;
+            }
+        }
+        __syncwarp();
+        warp_append(record, me, a.prov, a.n_prov);
+        if (a.stats) {
+            unsigned long long sl = st_leaves, sn = st_nodes, sc = st_cands, q = listed ? 1ull : 0ull;
+            for (int o = 16; o > 0; o >>= 1) {
+                sl += __shfl_xor_sync(kFull, sl, o);
+                sn += __shfl_xor_sync(kFull, sn, o);
+                sc += __shfl_xor_sync(kFull, sc, o);
+                q += __shfl_xor_sync(kFull, q, o);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(&a.stats[0], sl);
+                atomicAdd(&a.stats[1], sn);
+                atomicAdd(&a.stats[2], sc);
+                atomicAdd(&a.stats[3], 1ull);
+                atomicAdd(&a.stats[4], q);
+                atomicAdd(&a.stats[5], q);
+            }
+        }
+    }
+}
+
 
 // Launch of one shape; the grid covers the list's upper bound `a.n` with at
 // most four waves of resident blocks (the kernel strides over the rest).
@@ -320,6 +498,17 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
     if (b > cap) b = cap;
     if (b < 1) b = 1;
     k_cnns_t<D, CL, T, M, LEARN><<<(unsigned)b, T, 0, s>>>(a);
+}
+
+template <int D, bool CL>
+cudaError_t launch_knn(const CnnsArgs& a, uint64_t* kkey, uint32_t* kpos, int sms, cudaStream_t s)
+{
+    uint64_t b = ((uint64_t)a.n + 255) / 256;
+    const uint64_t cap = (uint64_t)sms * 3 * 4;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    k_knn_first<D, CL><<<(unsigned)b, 256, 0, s>>>(a, kkey, kpos);
+    return cudaGetLastError();
 }
 
 template <int D, bool CL, bool LEARN = false>

@@ -319,7 +319,8 @@ emst_status build_graph(emst_ctx* x)
                                     (const void*)(intptr_t)(c.learned ? 1 : 0), c.trace.p,
                                     (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p, c.snaps.p,
-                                    (const void*)(intptr_t)c.snap_cap};
+                                    (const void*)(intptr_t)c.snap_cap, c.kkey.p, c.kpos.p,
+                                    (const void*)(intptr_t)(c.knn_seed ? 1 : 0)};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
     cudaGraph_t g = nullptr, body = nullptr;
@@ -423,6 +424,7 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->search_shape > 0) c.search_shape = cfg->search_shape - 1;
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
         c.first_pass_ordered = cfg->first_pass_ordered != 0;
+        c.knn_seed = cfg->round1_neighbours >= 0;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);
@@ -469,6 +471,8 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.trace);
     emst::release(c.trace_ctl);
     emst::release(c.snaps);
+    emst::release(c.kkey);
+    emst::release(c.kpos);
     emst::release(c.sel_tmp);
     emst::release(c.lbp);
     emst::release(c.clb);

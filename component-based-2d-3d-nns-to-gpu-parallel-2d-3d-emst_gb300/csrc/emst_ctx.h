@@ -147,6 +147,11 @@ struct Ctx {
     // (one pass); with the query lists compacted before each pass, deferring
     // measured slower on GB300 for every factor tried (1.0001 .. 16)
     float first_pass_factor = INFINITY;
+    // round 1 keeps each point's kKnn nearest (k_knn_first); later rounds take
+    // the first entry outside the component without a search (k_reuse)
+    bool knn_seed = true;
+    DevBuf<uint64_t> kkey;  // n * kKnn keys (d2 bits << 32 | input id), sorted per point
+    DevBuf<uint32_t> kpos;  // n * kKnn leaf positions
     // one search launch per round: the points the factor keeps first, the
     // others after them (instead of a second pass)
     bool first_pass_ordered = false;
@@ -228,7 +233,11 @@ struct CnnsArgs {
     const int* round;  // rounds started (device)
     const uint32_t* list2;    // second segment of the same launch (ordered first pass), or null
     const uint32_t* n_list2;
+    bool knn_round1;          // round 1 runs k_knn_first (neighbour lists), not this kernel
 };
+
+// Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
+constexpr int kKnn = 8;
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the
@@ -254,6 +263,10 @@ cudaError_t proposal_trace_begin(Ctx& c);
 cudaError_t proposal_trace_end(Ctx& c);
 uint64_t splitmix(uint64_t& s);
 
+cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* kkey, uint32_t* kpos, int sms,
+                             cudaStream_t s);
+cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* kkey, uint32_t* kpos, int sms,
+                             cudaStream_t s);
 cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 

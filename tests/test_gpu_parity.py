@@ -315,6 +315,23 @@ def test_first_pass_rules_keep_edges(gpu_lib, kw, kind, dim):
         assert np.array_equal(e.round_stats(), ref_rounds)
 
 
+@pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 30000), ("uniform", 2, 30000), ("dups", 3, 8000),
+                                        ("lattice", 2, 5000), ("line", 3, 3000), ("dups", 2, 9)])
+def test_round1_neighbour_lists_keep_edges(gpu_lib, kind, dim, n):
+    """Round-1 neighbour lists (default) answer later rounds without changing
+    any edge or round, in the graph loop and the host loop."""
+    pts = family(kind, n, dim, 83)
+    out = []
+    for k in (-1, 0):
+        for host in (False, True):
+            with gpu_lib.Emst(round1_neighbours=k, host_rounds=host) as e:
+                uv, ln = e.solve(pts)
+                out.append((_canon(uv), ln, e.round_stats()))
+    for uv, ln, rs in out[1:]:
+        assert np.array_equal(uv, out[0][0]) and ln == pytest.approx(out[0][1], rel=1e-12)
+        assert np.array_equal(rs, out[0][2])
+
+
 def test_operator_order_is_checked(gpu_lib):
     with gpu_lib.Emst() as e:
         e.initialize(family("uniform", 100, 2, 1))
