@@ -237,7 +237,7 @@ struct CnnsArgs {
 };
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
-constexpr int kKnn = 8;
+constexpr int kKnn = 6;
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the

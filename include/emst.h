@@ -67,10 +67,10 @@ typedef struct {
     int first_pass_ordered; /* != 0: one search launch per round, the points
                               the factor keeps first and the others after
                               them, instead of a second pass */
-    int round1_neighbours; /* 0 = default: round 1 keeps each point's 8
+    int round1_neighbours; /* 0 = default: round 1 keeps each point's 6
                               nearest, and later rounds take the first one
                               outside the component without a search
-                              (8 x 12 bytes per point); -1 = off */
+                              (6 x 12 bytes per point); -1 = off */
     int reserved[1];
 } emst_config;
 
