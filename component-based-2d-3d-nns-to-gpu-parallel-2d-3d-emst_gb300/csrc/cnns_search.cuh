@@ -315,9 +315,20 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 // outside point -- every closer point is earlier in the list -- so most
 // points of rounds 2-4 need no search (k_reuse).  Entry 0 is the round-1
 // result, written like k_cnns_t's.  Runs only when the device round is 1.
+//
+// One warp per 32 consecutive queries of the list (in round 1 the list is
+// every point in leaf order, so a warp's queries are one leaf).  The warp
+// walks the tree together: its queries' own leaf first, then the sibling
+// subtree of each ancestor, a node entered when any lane's lower bound
+// reaches it.  A leaf is staged once in shared memory and every lane tests
+// all its points (broadcast reads), so all 32 lanes compute distances on
+// every candidate instead of diverging over per-lane traversals.  Each leaf
+// reaches every lane at most once, and a lane's bound only shrinks, so every
+// lane still sees every point within its final K-th distance: the lists are
+// the exact K nearest, as with one traversal per lane.
 template <int D, bool CL>
-__global__ void __launch_bounds__(256, 3) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ kkey,
-                                                       uint32_t* __restrict__ kpos)
+__global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ kkey,
+                                                                uint32_t* __restrict__ kpos)
 {
     if (*a.round != 1) return;
     const float4* __restrict__ spl = a.spl;
@@ -328,126 +339,150 @@ __global__ void __launch_bounds__(256, 3) k_knn_first(const CnnsArgs a, uint64_t
     const uint32_t n = a.n, L = a.L;
     const uint32_t* __restrict__ pcloud = a.pcloud;
     const uint32_t* __restrict__ ncloud = a.ncloud;
-    constexpr int K = kKnn, kTStack = 48;
+    constexpr int K = kKnn, kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
+    __shared__ float4 s_pt[kKnnWarps][32];
+    __shared__ uint32_t s_id[kKnnWarps][32];
+    __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
+    __shared__ uint32_t s_stack[kKnnWarps][kWStack];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* const pt = s_pt[w];
+    uint32_t* const ids = s_id[w];
+    uint32_t* const stack = s_stack[w];
     const uint32_t total = *a.n_list;
-    for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
-        const uint32_t qi = base0 + threadIdx.x;
+    const uint32_t stride = gridDim.x * kKnnWarps * 32;
+    for (uint32_t base0 = (blockIdx.x * kKnnWarps + w) * 32; base0 < total; base0 += stride) {
+        const uint32_t qi = base0 + lane;
         const bool listed = qi < total;
-        const uint32_t me = listed ? a.list[qi] : 0u;
+        const uint32_t me = a.list[listed ? qi : base0];
         const uint32_t labp = listed ? a.lab[me] : kEmpty;
-        bool record = false;
-        uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
-        if (listed) {
-            const float4 P = spl[me];
-            const int op = (int)perm[me];
-            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
-            uint64_t kk[K];
-            uint32_t kp[K];
+        const float4 P = spl[me];
+        const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
+        uint64_t kk[K];
+        uint32_t kp[K];
 #pragma unroll
-            for (int j = 0; j < K; ++j) {
-                kk[j] = kNoKey;
-                kp[j] = kNone;
+        for (int j = 0; j < K; ++j) {
+            kk[j] = kNoKey;
+            kp[j] = kNone;
+        }
+        // d2 of the K-th entry once the list is full; lanes past the list's
+        // end take -1 so that no node and no candidate is ever theirs
+        float bd = listed ? INFINITY : -1.f;
+        uint32_t st_leaves = 0, st_nodes = 0;
+
+        auto node_lb = [&](uint32_t node) -> float {
+            const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+            if (lo.x > hi.x) return INFINITY;
+            if (__ldg(&nlab[node]) == labp) return INFINITY;
+            if constexpr (CL) {
+                const uint32_t r = __ldg(&ncloud[node]);
+                if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
             }
-            float bd = INFINITY;  // d2 of the K-th entry once the list is full
-            auto offer = [&](uint32_t pos, float d2) {
-                if (d2 > bd) return;
-                const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | __ldg(&perm[pos]);
-                if (key >= kk[K - 1]) return;
+            const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+            const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+            const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+            return d2_of<D>(gx, gy, gz);
+        };
+        auto wanted = [&](float lb) { return lb < INFINITY && lb <= bd; };
+        // the whole warp scans one leaf: stage it in shared memory, let every
+        // lane mark the points within its bound (broadcast reads, no
+        // branches), then insert each lane's marked points -- the warp runs
+        // as many insert steps as its busiest lane needs, not one per point
+        // that any lane wants
+        auto scan_leaf = [&](uint32_t leaf) {
+            const uint32_t b = leaf * 32;
+            const uint32_t m = min(32u, n - b);
+            ++st_leaves;
+            __syncwarp();  // the previous leaf's reads are done
+            if ((uint32_t)lane < m) {
+                pt[lane] = __ldg(&spl[b + lane]);
+                ids[lane] = __ldg(&perm[b + lane]);
+                if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
+            } else {
+                // past the last point: NaN coordinates fail every d2 <= bound test
+                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(labp));
+                if constexpr (CL) s_cl[w][lane] = ~0u;
+            }
+            __syncwarp();
+            uint32_t mask = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float4 c = pt[j];
+                const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                // a candidate in the query's component (itself) or, in a
+                // batch, in another cloud (lanes may hold different clouds)
+                bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
+                if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                mask |= (ok ? 1u : 0u) << j;
+            }
+            while (mask) {
+                const int j = __ffs(mask) - 1;
+                mask &= mask - 1u;
+                const float4 c = pt[j];
+                const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                if (d2 > bd) continue;
+                const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | ids[j];
+                if (key >= kk[K - 1]) continue;
+                const uint32_t pos = b + j;
                 // sorted insert, all in registers
 #pragma unroll
-                for (int j = K - 1; j > 0; --j) {
-                    const bool sh = key < kk[j - 1];
-                    const bool put = !sh && key < kk[j];
-                    kk[j] = sh ? kk[j - 1] : (put ? key : kk[j]);
-                    kp[j] = sh ? kp[j - 1] : (put ? pos : kp[j]);
+                for (int t = K - 1; t > 0; --t) {
+                    const bool sh = key < kk[t - 1];
+                    const bool put = !sh && key < kk[t];
+                    kk[t] = sh ? kk[t - 1] : (put ? key : kk[t]);
+                    kp[t] = sh ? kp[t - 1] : (put ? pos : kp[t]);
                 }
                 if (key < kk[0]) {
                     kk[0] = key;
                     kp[0] = pos;
                 }
                 if (kk[K - 1] != kNoKey) bd = __uint_as_float((uint32_t)(kk[K - 1] >> 32));
-            };
-            auto scan_leaf = [&](uint32_t leaf) {
-                const uint32_t b = leaf * 32;
-                if (b >= n) return;
-                const uint32_t m = min(32u, n - b);
-                ++st_leaves;
-                st_cands += m;
-                bool mixed = false;
-                if constexpr (CL) {
-                    const uint32_t r = __ldg(&ncloud[L + leaf]);
-                    mixed = (r >> 16) != (r & 0xffffu);
-                }
-                for (uint32_t j = 0; j < m; j += 4) {
-                    float4 c[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, __uint_as_float(labp));
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        if (__float_as_uint(c[k].w) == labp) continue;
-                        if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
-                        offer(b + j + k,
-                              d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z)));
-                    }
-                }
-            };
-            auto node_lb = [&](uint32_t node) -> float {
-                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
-                if (lo.x > hi.x) return INFINITY;
-                if (__ldg(&nlab[node]) == labp) return INFINITY;
-                if constexpr (CL) {
-                    const uint32_t r = __ldg(&ncloud[node]);
-                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
-                }
-                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
-                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
-                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
-                return d2_of<D>(gx, gy, gz);
-            };
-            const uint32_t own = me >> 5;
-            scan_leaf(own);
-            uint32_t stack[kTStack];
-            for (uint32_t v = L + own; v > 1; v >>= 1) {
-                const uint32_t sib = v ^ 1u;
-                ++st_nodes;
-                const float ls = node_lb(sib);
-                if (!(ls < INFINITY) || ls > bd) continue;
-                int top = 0;
-                stack[top++] = sib;
-                while (top > 0) {
-                    uint32_t leaf = kNone;
-                    while (top > 0) {
-                        const uint32_t node = stack[--top];
-                        ++st_nodes;
-                        if (node >= L) {
-                            const float lb = node_lb(node);
-                            if (!(lb < INFINITY) || lb > bd) continue;
-                            leaf = node - L;
-                            break;
-                        }
-                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                        const float l0 = node_lb(c0), l1 = node_lb(c1);
-                        const bool near0 = l0 <= l1;
-                        const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
-                        const float ln = near0 ? l0 : l1, lf = near0 ? l1 : l0;
-                        if (top + 2 > kTStack) {  // cannot happen for trees of depth < 46
-                            top = 0;
-                            break;
-                        }
-                        if (lf < INFINITY && lf <= bd) stack[top++] = cf;
-                        if (ln < INFINITY && ln <= bd) stack[top++] = cn;
-                    }
-                    if (leaf != kNone) scan_leaf(leaf);
-                }
             }
+        };
+
+        // the warp's own leaf (lane 0's query's) first, then bottom-up: every
+        // other leaf lies in exactly one sibling subtree of its ancestors
+        const uint32_t own = __shfl_sync(kFull, me, 0) >> 5;
+        scan_leaf(own);
+        for (uint32_t v = L + own; v > 1; v >>= 1) {
+            const uint32_t sib = v ^ 1u;
+            ++st_nodes;
+            if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
+            int top = 0;
+            stack[top++] = sib;
+            while (top > 0) {
+                const uint32_t node = stack[--top];
+                ++st_nodes;
+                if (node >= L) {
+                    // bounds re-checked: they may have shrunk since the push
+                    if (__any_sync(kFull, wanted(node_lb(node)))) scan_leaf(node - L);
+                    continue;
+                }
+                const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                const float l0 = node_lb(c0), l1 = node_lb(c1);
+                const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
+                // the child nearer to the warp's nearest lane is searched next
+                const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
+                const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
+                const bool near0 = m0 <= m1;
+                const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
+                __syncwarp();  // every lane has read the popped entry
+                if (wf) stack[top++] = near0 ? c1 : c0;
+                if (wn) stack[top++] = near0 ? c0 : c1;
+                __syncwarp();
+            }
+        }
+        if (listed) {
 #pragma unroll
             for (int j = 0; j < K; ++j) {
                 kkey[(size_t)me * K + j] = kk[j];
                 kpos[(size_t)me * K + j] = kp[j];
             }
-            // round-1 result: entry 0 (exact: every node within the K-th
-            // distance was searched)
+        }
+        // round-1 result: entry 0 (exact: every node within the K-th
+        // distance was searched)
+        bool record = false;
+        if (listed) {
+            const int op = (int)__ldg(&perm[me]);
             if (kk[0] != kNoKey) {
                 const float d0 = __uint_as_float((uint32_t)(kk[0] >> 32));
                 const uint32_t mn = (uint32_t)min(op, (int)(uint32_t)kk[0]);
@@ -467,17 +502,12 @@ __global__ void __launch_bounds__(256, 3) k_knn_first(const CnnsArgs a, uint64_t
         __syncwarp();
         warp_append(record, me, a.prov, a.n_prov);
         if (a.stats) {
-            unsigned long long sl = st_leaves, sn = st_nodes, sc = st_cands, q = listed ? 1ull : 0ull;
-            for (int o = 16; o > 0; o >>= 1) {
-                sl += __shfl_xor_sync(kFull, sl, o);
-                sn += __shfl_xor_sync(kFull, sn, o);
-                sc += __shfl_xor_sync(kFull, sc, o);
-                q += __shfl_xor_sync(kFull, q, o);
-            }
-            if ((threadIdx.x & 31) == 0) {
-                atomicAdd(&a.stats[0], sl);
-                atomicAdd(&a.stats[1], sn);
-                atomicAdd(&a.stats[2], sc);
+            // leaves and nodes are per warp; candidates per listed lane
+            unsigned long long q = __popc(__ballot_sync(kFull, listed));
+            if (lane == 0) {
+                atomicAdd(&a.stats[0], (unsigned long long)st_leaves);
+                atomicAdd(&a.stats[1], (unsigned long long)st_nodes * 32ull);
+                atomicAdd(&a.stats[2], (unsigned long long)st_leaves * 32ull * q);
                 atomicAdd(&a.stats[3], 1ull);
                 atomicAdd(&a.stats[4], q);
                 atomicAdd(&a.stats[5], q);
@@ -503,11 +533,12 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 template <int D, bool CL>
 cudaError_t launch_knn(const CnnsArgs& a, uint64_t* kkey, uint32_t* kpos, int sms, cudaStream_t s)
 {
-    uint64_t b = ((uint64_t)a.n + 255) / 256;
-    const uint64_t cap = (uint64_t)sms * 3 * 4;
+    constexpr int T = kKnnWarps * 32;
+    uint64_t b = ((uint64_t)a.n + T - 1) / T;
+    const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL><<<(unsigned)b, 256, 0, s>>>(a, kkey, kpos);
+    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, kkey, kpos);
     return cudaGetLastError();
 }
 

@@ -238,6 +238,7 @@ struct CnnsArgs {
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
 constexpr int kKnn = 6;
+constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the
