@@ -383,12 +383,17 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             return d2_of<D>(gx, gy, gz);
         };
         auto wanted = [&](float lb) { return lb < INFINITY && lb <= bd; };
-        // the whole warp scans one leaf: stage it in shared memory, let every
-        // lane mark the points within its bound (broadcast reads, no
-        // branches), then insert each lane's marked points -- the warp runs
-        // as many insert steps as its busiest lane needs, not one per point
-        // that any lane wants
-        auto scan_leaf = [&](uint32_t leaf) {
+        // the whole warp scans one leaf, wanted by the lanes in `need`: stage
+        // it in shared memory, mark each wanting lane's points within its
+        // bound, then insert each lane's marked points -- the warp runs as
+        // many insert steps as its busiest lane needs, not one per point that
+        // any lane wants.  Marking: with many wanting lanes, every lane tests
+        // all 32 points (broadcast reads); with few, the points sit one per
+        // lane and each wanting query is tested against all of them at once
+        // (one ballot per query).  A lane that does not want the leaf has no
+        // point in it within its bound (the box bound never exceeds a
+        // point's d2: both round the same differences the same way).
+        auto scan_leaf = [&](uint32_t leaf, uint32_t need) {
             const uint32_t b = leaf * 32;
             const uint32_t m = min(32u, n - b);
             ++st_leaves;
@@ -404,15 +409,36 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             }
             __syncwarp();
             uint32_t mask = 0;
+            if (__popc(need) > kKnnDense) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const float4 c = pt[j];
-                const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                // a candidate in the query's component (itself) or, in a
-                // batch, in another cloud (lanes may hold different clouds)
-                bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
-                if constexpr (CL) ok = ok && s_cl[w][j] == qc;
-                mask |= (ok ? 1u : 0u) << j;
+                for (int j = 0; j < 32; ++j) {
+                    const float4 c = pt[j];
+                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                    // not a candidate: in the query's component (itself) or,
+                    // in a batch, in another cloud (lanes may hold different
+                    // clouds)
+                    bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
+                    if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                    mask |= (ok ? 1u : 0u) << j;
+                }
+            } else {
+                const float4 c = pt[lane];
+                const uint32_t cc = CL ? s_cl[w][lane] : 0u;
+                while (need) {
+                    const int q = __ffs(need) - 1;
+                    need &= need - 1u;
+                    const float qx = __shfl_sync(kFull, P.x, q), qy = __shfl_sync(kFull, P.y, q);
+                    const float qz = D == 3 ? __shfl_sync(kFull, P.z, q) : 0.f;
+                    const float qb = __shfl_sync(kFull, bd, q);
+                    const uint32_t ql = __shfl_sync(kFull, labp, q);
+                    // every lane takes part in every shuffle (none under a condition)
+                    const uint32_t qq = CL ? __shfl_sync(kFull, qc, q) : 0u;
+                    const float d2 = d2_of<D>(__fsub_rn(c.x, qx), __fsub_rn(c.y, qy), __fsub_rn(c.z, qz));
+                    bool ok = d2 <= qb && __float_as_uint(c.w) != ql;
+                    if constexpr (CL) ok = ok && cc == qq;
+                    const uint32_t mb = __ballot_sync(kFull, ok);
+                    if (lane == q) mask = mb;
+                }
             }
             while (mask) {
                 const int j = __ffs(mask) - 1;
@@ -442,7 +468,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         // the warp's own leaf (lane 0's query's) first, then bottom-up: every
         // other leaf lies in exactly one sibling subtree of its ancestors
         const uint32_t own = __shfl_sync(kFull, me, 0) >> 5;
-        scan_leaf(own);
+        scan_leaf(own, __ballot_sync(kFull, bd >= 0.f));
         for (uint32_t v = L + own; v > 1; v >>= 1) {
             const uint32_t sib = v ^ 1u;
             ++st_nodes;
@@ -454,7 +480,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 ++st_nodes;
                 if (node >= L) {
                     // bounds re-checked: they may have shrunk since the push
-                    if (__any_sync(kFull, wanted(node_lb(node)))) scan_leaf(node - L);
+                    const uint32_t need = __ballot_sync(kFull, wanted(node_lb(node)));
+                    if (need) scan_leaf(node - L, need);
                     continue;
                 }
                 const uint32_t c0 = 2 * node, c1 = c0 + 1;

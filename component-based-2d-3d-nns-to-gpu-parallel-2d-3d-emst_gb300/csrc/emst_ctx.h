@@ -239,6 +239,7 @@ struct CnnsArgs {
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
 constexpr int kKnn = 6;
 constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
+constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the
