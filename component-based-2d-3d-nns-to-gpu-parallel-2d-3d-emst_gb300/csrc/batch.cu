@@ -7,7 +7,7 @@
 //     get z = 0, and fma(0, 0, r) == r, so their squared distances are the 2D
 //     ones bit for bit;
 //   * the cell key carries the cloud index (cb = ceil(log2 clouds) bits) above
-//     a Morton code of the remaining 63 - cb bits (e.g. 18 bits/axis in 3D and
+//     a Hilbert index of the remaining 63 - cb bits (e.g. 18 bits/axis in 3D and
 //     27 bits/axis in 2D for 512 clouds), so every cloud is a contiguous run of
 //     leaves;
 //   * every tree node records the cloud all its points belong to (or MIXED);
@@ -32,7 +32,7 @@ namespace {
 constexpr int kThreads = 256;
 
 // One block per cloud: min/max, unitX (the reference formula for that
-// cloud's size and dimension) and the Morton quantisation scale.
+// cloud's size and dimension) and the cell quantisation scale.
 __global__ void k_batch_norm(const float* __restrict__ in, const int64_t* __restrict__ off,
                              const int64_t* __restrict__ foff, const int32_t* __restrict__ dims,
                              NormParams* __restrict__ np, DevCounters* __restrict__ ctr, int bits3, int bits2)
@@ -102,7 +102,7 @@ __global__ void k_batch_norm(const float* __restrict__ in, const int64_t* __rest
 }
 
 // One block per cloud: rescale (float(float(p - pMin) * float(unitX))), key
-// (cloud << shift | Morton), staging float4 (x, y, z or 0, global id).
+// (cloud << shift | Hilbert index), staging float4 (x, y, z or 0, global id).
 __global__ void k_batch_rescale_key(const float* __restrict__ in, const int64_t* __restrict__ off,
                                     const int64_t* __restrict__ foff, const int32_t* __restrict__ dims,
                                     const NormParams* __restrict__ np, float4* __restrict__ stage,
@@ -116,14 +116,14 @@ __global__ void k_batch_rescale_key(const float* __restrict__ in, const int64_t*
     const NormParams q = np[c];
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         float s[3] = {0.f, 0.f, 0.f};
-        uint64_t m = 0;
+        uint32_t cell[3] = {0u, 0u, 0u};
         for (int k = 0; k < D; ++k) {
             s[k] = __fmul_rn(__fsub_rn(p[i * D + k], q.pmin[k]), q.uxf);
             const uint32_t qmax = (1u << (D == 3 ? bits3 : bits2)) - 1u;
             // float(qmax) may round up to 2^bits: clamp again after the conversion
-            const uint32_t qq = min((uint32_t)fminf(fmaxf(__fmul_rn(s[k], q.qscale), 0.f), (float)qmax), qmax);
-            m |= (D == 3 ? spread3(qq) : spread2(qq)) << k;
+            cell[k] = min((uint32_t)fminf(fmaxf(__fmul_rn(s[k], q.qscale), 0.f), (float)qmax), qmax);
         }
+        const uint64_t m = D == 3 ? hilbert_index<3>(cell, bits3) : hilbert_index<2>(cell, bits2);
         const int64_t g = b + i;
         stage[g] = make_float4(s[0], s[1], s[2], __int_as_float((int)g));
         key[g] = ((uint64_t)c << shift) | m;

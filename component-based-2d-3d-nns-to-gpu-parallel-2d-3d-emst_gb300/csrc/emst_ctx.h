@@ -4,7 +4,7 @@
 // HBM layout (all arrays indexed by position in leaf order unless noted):
 //   in        n*dim float   caller's points, input order (original frame)
 //   scaled    n*dim float   rescaled points, input order
-//   sp        n float4      rescaled points in leaf (Morton) order, .w = input id
+//   sp        n float4      rescaled points in leaf (Hilbert) order, .w = input id
 //   perm      n uint32      leaf position -> input id
 //   nlo/nhi   2L float4     bounding boxes of the implicit leaf tree (heap order)
 //   nid       2L int4       per node: two smallest input ids and their leaf positions
@@ -56,7 +56,7 @@ struct NormParams {
     float pmin[3];
     float pmax[3];
     float uxf;       // float(unitX)
-    float qscale;    // Morton quantisation scale
+    float qscale;    // cell quantisation scale
     double unitx;    // unitX as the reference computes it (double)
     float smax[3];   // rescaled maxima
     float pad;

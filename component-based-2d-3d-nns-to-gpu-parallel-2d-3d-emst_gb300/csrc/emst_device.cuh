@@ -132,7 +132,7 @@ __device__ __forceinline__ bool cone_hits(int r, const float* a, const float* b)
     return true;
 }
 
-// 64-bit Morton codes.
+// Bit spreading: bit b of x moves to bit 2b (spread2) or 3b (spread3).
 __device__ __forceinline__ uint64_t spread2(uint32_t x)
 {
     uint64_t v = x;
@@ -152,6 +152,41 @@ __device__ __forceinline__ uint64_t spread3(uint32_t x)
     v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
     v = (v | (v << 2)) & 0x1249249249249249ull;
     return v;
+}
+
+// Hilbert index of the cell x[0..D) (bits per axis), after J. Skilling,
+// "Programming the Hilbert curve", AIP Conf. Proc. 707, 381 (2004): the
+// coordinates are turned in place into the transposed index, whose bits,
+// interleaved with axis 0 most significant in each group, form the index.
+// Cells with consecutive indices share a face, so a run of 32 consecutive
+// points has a compact bounding box; a Z-order run can jump across the
+// domain and leave a box that overlaps many others.
+template <int D>
+__device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3], int bits)
+{
+    const uint32_t top = 1u << (bits - 1);
+    for (uint32_t q = top; q > 1; q >>= 1) {
+        const uint32_t p = q - 1;
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            if (x[i] & q) {
+                x[0] ^= p;  // invert the low bits
+            } else {
+                const uint32_t t = (x[0] ^ x[i]) & p;  // exchange the low bits
+                x[0] ^= t;
+                x[i] ^= t;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 1; i < D; ++i) x[i] ^= x[i - 1];  // Gray encode
+    uint32_t t = 0;
+    for (uint32_t q = top; q > 1; q >>= 1)
+        if (x[D - 1] & q) t ^= q - 1;
+#pragma unroll
+    for (int i = 0; i < D; ++i) x[i] ^= t;
+    if (D == 3) return (spread3(x[0]) << 2) | (spread3(x[1]) << 1) | spread3(x[2]);
+    return (spread2(x[0]) << 1) | spread2(x[1]);
 }
 
 }  // namespace emst

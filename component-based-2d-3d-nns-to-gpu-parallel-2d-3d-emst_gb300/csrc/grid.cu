@@ -7,7 +7,7 @@
 //      InputRW.h:545-559) and the reference's unitX in double
 //      (SolutionEMST.cu:305-341);
 //   2. the rescale p' = float(float(p - pMin) * float(unitX)) (:361-364),
-//      fused with a 64-bit Morton cell key per point (21 bits/axis in 3D,
+//      fused with a 64-bit Hilbert cell key per point (21 bits/axis in 3D,
 //      31 bits/axis in 2D);
 //   3. a radix sort of the cell keys, so points of one cell (and of
 //      neighbouring cells) are contiguous: leaves of 32 consecutive points
@@ -86,7 +86,7 @@ __global__ void k_minmax_part(const float* __restrict__ in, int64_t n, float* __
 }
 
 // Stage 2 (one block): final min/max, unitX (double, as SolutionEMST.cu:305-341),
-// rescaled extents and the Morton quantisation scale.
+// rescaled extents and the cell quantisation scale.
 template <int D>
 __global__ void k_minmax_final(const float* __restrict__ part, int nblk, int64_t n, NormParams* __restrict__ np)
 {
@@ -144,7 +144,7 @@ __global__ void k_minmax_final(const float* __restrict__ part, int nblk, int64_t
     np->qscale = smax > 0.f ? qmax / smax : 0.f;
 }
 
-// Rescale (SolutionEMST.cu:361-364) + Morton cell key.
+// Rescale (SolutionEMST.cu:361-364) + Hilbert cell key.
 template <int D>
 __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const NormParams* __restrict__ np,
                               float* __restrict__ scaled, uint64_t* __restrict__ key, uint32_t* __restrict__ idx)
@@ -152,16 +152,15 @@ __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const Nor
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float uxf = np->uxf, qs = np->qscale;
-    uint64_t k = 0;
+    uint32_t cell[3] = {0u, 0u, 0u};
 #pragma unroll
     for (int c = 0; c < D; ++c) {
         float s = __fmul_rn(__fsub_rn(in[i * D + c], np->pmin[c]), uxf);
         scaled[i * D + c] = s;
         float qf = fminf(fmaxf(__fmul_rn(s, qs), 0.f), D == 3 ? 2097151.f : 2147483520.f);
-        uint32_t q = (uint32_t)qf;
-        k |= (D == 3 ? spread3(q) : spread2(q)) << c;
+        cell[c] = (uint32_t)qf;
     }
-    key[i] = k;
+    key[i] = hilbert_index<D>(cell, D == 3 ? 21 : 31);
     idx[i] = (uint32_t)i;
 }
 

@@ -6,7 +6,7 @@
 // pattern of the other axes) the nearest point of R under (d2, input id).
 //
 // Design: one warp per query tile.  A tile is one leaf of 32 consecutive
-// points in Morton order, so the 32 lanes hold 32 spatially close queries.
+// points in Hilbert order, so the 32 lanes hold 32 spatially close queries.
 // The warp walks the implicit leaf tree depth-first (near child first); a
 // node is opened when any lane may still improve a region from it:
 //   * lower bound lb2 of d2 from the lane's query to the node's box, computed
