@@ -104,7 +104,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag, uint32_t* __restrict__ prov,
                         uint32_t* __restrict__ n_prov, const int* __restrict__ round,
                         const uint64_t* __restrict__ kkey, const uint32_t* __restrict__ kpos,
-                        const uint32_t* __restrict__ perm)
+                        unsigned char* __restrict__ kcur, const uint32_t* __restrict__ perm)
 {
     const bool lists = kkey && *round >= 2;  // round 1 builds them
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -120,9 +120,14 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                 uint32_t lb = __float_as_uint(lbp[p]);
                 if (lists && lb != 0x7f800000u) {
                     // the first neighbour outside the component is the exact
-                    // nearest outside point: every closer point precedes it
+                    // nearest outside point: every closer point precedes it.
+                    // Entries before the cursor were found inside the
+                    // component in an earlier round and stay inside
+                    // (components only grow); their d2 is already in lbp.
                     bool full = true;
-                    for (int j = 0; j < kKnn; ++j) {
+                    const int j0 = kcur[p];
+                    int j = j0;
+                    for (; j < kKnn; ++j) {
                         const uint64_t kj = kkey[(size_t)p * kKnn + j];
                         if (kj == kNoKey) {
                             full = false;
@@ -139,9 +144,11 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         }
                         lb = max(lb, (uint32_t)(kj >> 32));  // non-negative floats order as their bits
                     }
-                    if (key == kNoKey) {
+                    if (j != j0) kcur[p] = (unsigned char)j;
+                    if (key == kNoKey && (j != j0 || !full)) {
                         // none outside: a full list bounds the distance from below;
                         // a short one held every other point of the cloud
+                        // (an exhausted list, j0 == kKnn, adds nothing new)
                         lb = full ? lb : 0x7f800000u;
                         lbp[p] = __uint_as_float(lb);
                     }
@@ -474,6 +481,7 @@ cudaError_t cnns_init(Ctx& c)
     if (c.knn_seed && !c.cnns_warp) {
         if ((e = ensure(c.kkey, n * kKnn)) != cudaSuccess) return e;
         if ((e = ensure(c.kpos, n * kKnn)) != cudaSuccess) return e;
+        if ((e = ensure(c.kcur, n)) != cudaSuccess) return e;
     }
     size_t tb = 0, tb2 = 0;
     if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
@@ -498,7 +506,7 @@ cudaError_t cnns_select(Ctx& c)
     const bool knn = c.knn_seed && !c.cnns_warp;
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
                                                   c.clb.p, c.dflag.p, c.prov.p, &d->n_prov, &d->round,
-                                                  knn ? c.kkey.p : nullptr, c.kpos.p, c.perm.p);
+                                                  knn ? c.kkey.p : nullptr, c.kpos.p, c.kcur.p, c.perm.p);
     // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
     cudaError_t e;
@@ -554,8 +562,8 @@ cudaError_t cnns_select(Ctx& c)
                 if (et != cudaSuccess) return et;
             }
             if (knn && pass == 1) {  // round 1 only (decided on the device)
-                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.kkey.p, c.kpos.p, c.sms, c.stream)
-                                            : launch_knn_first3(a, pc != nullptr, c.kkey.p, c.kpos.p, c.sms, c.stream);
+                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.kkey.p, c.kpos.p, c.kcur.p, c.sms, c.stream)
+                                            : launch_knn_first3(a, pc != nullptr, c.kkey.p, c.kpos.p, c.kcur.p, c.sms, c.stream);
                 if (ek != cudaSuccess) return ek;
                 c.launches++;
             }

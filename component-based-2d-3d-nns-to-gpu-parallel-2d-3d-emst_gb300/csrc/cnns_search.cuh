@@ -328,7 +328,8 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 // the exact K nearest, as with one traversal per lane.
 template <int D, bool CL>
 __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ kkey,
-                                                                uint32_t* __restrict__ kpos)
+                                                                uint32_t* __restrict__ kpos,
+                                                                unsigned char* __restrict__ kcur)
 {
     if (*a.round != 1) return;
     const float4* __restrict__ spl = a.spl;
@@ -504,6 +505,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 kkey[(size_t)me * K + j] = kk[j];
                 kpos[(size_t)me * K + j] = kp[j];
             }
+            kcur[me] = 0;
         }
         // round-1 result: entry 0 (exact: every node within the K-th
         // distance was searched)
@@ -558,14 +560,14 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 }
 
 template <int D, bool CL>
-cudaError_t launch_knn(const CnnsArgs& a, uint64_t* kkey, uint32_t* kpos, int sms, cudaStream_t s)
+cudaError_t launch_knn(const CnnsArgs& a, uint64_t* kkey, uint32_t* kpos, unsigned char* kcur, int sms, cudaStream_t s)
 {
     constexpr int T = kKnnWarps * 32;
     uint64_t b = ((uint64_t)a.n + T - 1) / T;
     const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, kkey, kpos);
+    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, kkey, kpos, kcur);
     return cudaGetLastError();
 }
 
