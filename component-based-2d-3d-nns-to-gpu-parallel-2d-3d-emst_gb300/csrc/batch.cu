@@ -123,7 +123,8 @@ __global__ void k_batch_rescale_key(const float* __restrict__ in, const int64_t*
             // float(qmax) may round up to 2^bits: clamp again after the conversion
             cell[k] = min((uint32_t)fminf(fmaxf(__fmul_rn(s[k], q.qscale), 0.f), (float)qmax), qmax);
         }
-        const uint64_t m = D == 3 ? hilbert_index<3>(cell, bits3) : hilbert_index<2>(cell, bits2);
+        // cells below 2^bits per axis: the index fits in D * bits <= shift bits
+        const uint64_t m = D == 3 ? hilbert_index<3>(cell) : hilbert_index<2>(cell);
         const int64_t g = b + i;
         stage[g] = make_float4(s[0], s[1], s[2], __int_as_float((int)g));
         key[g] = ((uint64_t)c << shift) | m;

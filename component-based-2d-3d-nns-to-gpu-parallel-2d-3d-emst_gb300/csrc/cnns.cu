@@ -26,6 +26,7 @@
 // reference order restricted to that query, so each component's minimum --
 // and with it every round's edge set -- equals the static-table method's.
 #include <climits>
+#include <cmath>
 
 #include <cub/device/device_select.cuh>
 #include <thrust/iterator/counting_iterator.h>
@@ -103,10 +104,10 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         uint64_t* __restrict__ selkey, float* __restrict__ lbp, uint64_t* __restrict__ ckey,
                         uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag, uint32_t* __restrict__ prov,
                         uint32_t* __restrict__ n_prov, const int* __restrict__ round,
-                        const uint64_t* __restrict__ kkey, const uint32_t* __restrict__ kpos,
-                        unsigned char* __restrict__ kcur, const uint32_t* __restrict__ perm)
+                        const uint64_t* __restrict__ klist, unsigned char* __restrict__ kcur,
+                        const uint32_t* __restrict__ perm)
 {
-    const bool lists = kkey && *round >= 2;  // round 1 builds them
+    const bool lists = klist && *round >= 2;  // round 1 builds them
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool is_dirty = false, record = false;
@@ -128,14 +129,14 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     const int j0 = kcur[p];
                     int j = j0;
                     for (; j < kKnn; ++j) {
-                        const uint64_t kj = kkey[(size_t)p * kKnn + j];
-                        if (kj == kNoKey) {
+                        const uint64_t kj = klist[(size_t)j * n + p];  // d2 bits << 32 | position
+                        const uint32_t qj = (uint32_t)kj;
+                        if (qj == kNone) {
                             full = false;
                             break;
                         }
-                        const uint32_t qj = kpos[(size_t)p * kKnn + j];
                         if (lab[qj] != lp) {
-                            const uint32_t mn = min(perm[p], (uint32_t)kj);
+                            const uint32_t mn = min(perm[p], perm[qj]);
                             key = (kj & 0xffffffff00000000ull) | mn;
                             selq[p] = qj;
                             selkey[p] = key;
@@ -479,8 +480,7 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
     if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
     if (c.knn_seed && !c.cnns_warp) {
-        if ((e = ensure(c.kkey, n * kKnn)) != cudaSuccess) return e;
-        if ((e = ensure(c.kpos, n * kKnn)) != cudaSuccess) return e;
+        if ((e = ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
         if ((e = ensure(c.kcur, n)) != cudaSuccess) return e;
     }
     size_t tb = 0, tb2 = 0;
@@ -506,7 +506,8 @@ cudaError_t cnns_select(Ctx& c)
     const bool knn = c.knn_seed && !c.cnns_warp;
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
                                                   c.clb.p, c.dflag.p, c.prov.p, &d->n_prov, &d->round,
-                                                  knn ? c.kkey.p : nullptr, c.kpos.p, c.kcur.p, c.perm.p);
+                                                  knn ? c.klist.p : nullptr, c.kcur.p, c.perm.p);
+    c.launches++;
     // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
     cudaError_t e;
@@ -515,6 +516,7 @@ cudaError_t cnns_select(Ctx& c)
         size_t tb = c.sel_tmp.cap;
         e = cub::DeviceSelect::Flagged(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
                                        &d->n_dirty, (int)c.n, c.stream);
+        c.launches += 2;  // a CUB selection is two kernels
     } else {
         // the learned proposal makes the first-pass choice itself
         const float first_factor = c.learned && !c.n_clouds ? INFINITY : c.first_pass_factor;
@@ -522,15 +524,22 @@ cudaError_t cnns_select(Ctx& c)
                                                               c.clb.p, first_factor, st);
         c.launches++;
         e = select_flagged_one(c, c.dirty.p, &d->n_dirty);
-        if (e == cudaSuccess && c.first_pass_ordered && !(c.learned && !c.n_clouds))
+        c.launches += 2;
+        if (e == cudaSuccess && c.first_pass_ordered && !(c.learned && !c.n_clouds)) {
             e = select_flagged_two(c, c.dirty2.p, &d->n_dirty2);
+            c.launches += 2;
+        }
     }
     if (e != cudaSuccess) return e;
     constexpr int WPB = 4;
     const unsigned blocks = (unsigned)std::min<int64_t>((c.n + 32 * WPB - 1) / (32 * WPB), 152 * 32);
     const uint32_t* pc = c.n_clouds ? c.pcloud.p : nullptr;
     const uint32_t* nc = c.n_clouds ? c.ncloud.p : nullptr;
-    for (int pass = 1; pass <= 2; ++pass) {
+    // A second pass has work only if something can defer a point: a finite
+    // first-pass factor, the learned proposal (single clouds), or the warp
+    // search's defer list.  Otherwise it is left out of the round.
+    const bool two_passes = c.cnns_warp || (c.learned && !pc) || !std::isinf(c.first_pass_factor);
+    for (int pass = 1; pass <= (two_passes ? 2 : 1); ++pass) {
         const uint32_t* list = pass == 1 ? c.dirty.p : c.dirty2.p;
         const uint32_t* cnt = pass == 1 ? &d->n_dirty : &d->n_dirty2;
         if (c.cnns_warp) {
@@ -562,25 +571,26 @@ cudaError_t cnns_select(Ctx& c)
                 if (et != cudaSuccess) return et;
             }
             if (knn && pass == 1) {  // round 1 only (decided on the device)
-                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.kkey.p, c.kpos.p, c.kcur.p, c.sms, c.stream)
-                                            : launch_knn_first3(a, pc != nullptr, c.kkey.p, c.kpos.p, c.kcur.p, c.sms, c.stream);
+                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream)
+                                            : launch_knn_first3(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream);
                 if (ek != cudaSuccess) return ek;
                 c.launches++;
             }
             cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
-            if (pass == 1 && !ordered) {
+            if (pass == 1 && !ordered && two_passes) {
                 k_filter_second<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p,
                                                                              c.lbp.p, c.ckey.p);
                 c.launches++;
                 cudaError_t e2 = select_flagged_one(c, c.dirty2.p, &d->n_dirty2);
                 if (e2 != cudaSuccess) return e2;
+                c.launches += 2;
             }
         }
         c.nns_launches++;
+        c.launches++;
     }
-    c.launches += 3;
     if (c.trace_cap > 0 && !(c.learned && !pc)) {
         cudaError_t et = proposal_trace_end(c);
         if (et != cudaSuccess) return et;

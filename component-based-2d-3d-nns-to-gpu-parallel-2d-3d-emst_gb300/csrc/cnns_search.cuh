@@ -327,8 +327,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 // lane still sees every point within its final K-th distance: the lists are
 // the exact K nearest, as with one traversal per lane.
 template <int D, bool CL>
-__global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ kkey,
-                                                                uint32_t* __restrict__ kpos,
+__global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ klist,
                                                                 unsigned char* __restrict__ kcur)
 {
     if (*a.round != 1) return;
@@ -501,10 +500,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         }
         if (listed) {
 #pragma unroll
-            for (int j = 0; j < K; ++j) {
-                kkey[(size_t)me * K + j] = kk[j];
-                kpos[(size_t)me * K + j] = kp[j];
-            }
+            for (int j = 0; j < K; ++j)
+                klist[(size_t)j * n + me] = kk[j] == kNoKey ? ~0ull : ((kk[j] >> 32) << 32) | kp[j];
             kcur[me] = 0;
         }
         // round-1 result: entry 0 (exact: every node within the K-th
@@ -560,14 +557,14 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 }
 
 template <int D, bool CL>
-cudaError_t launch_knn(const CnnsArgs& a, uint64_t* kkey, uint32_t* kpos, unsigned char* kcur, int sms, cudaStream_t s)
+cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, int sms, cudaStream_t s)
 {
     constexpr int T = kKnnWarps * 32;
     uint64_t b = ((uint64_t)a.n + T - 1) / T;
     const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, kkey, kpos, kcur);
+    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, klist, kcur);
     return cudaGetLastError();
 }
 

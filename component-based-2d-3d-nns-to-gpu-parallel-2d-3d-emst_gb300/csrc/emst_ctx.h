@@ -150,8 +150,9 @@ struct Ctx {
     // round 1 keeps each point's kKnn nearest (k_knn_first); later rounds take
     // the first entry outside the component without a search (k_reuse)
     bool knn_seed = true;
-    DevBuf<uint64_t> kkey;  // n * kKnn keys (d2 bits << 32 | input id), sorted per point
-    DevBuf<uint32_t> kpos;  // n * kKnn leaf positions
+    // kKnn entries per point, entry-major (entry j of point p at j * n + p):
+    // d2 bits << 32 | leaf position, sorted by (d2, input id); ~0 = no entry
+    DevBuf<uint64_t> klist;
     DevBuf<unsigned char> kcur;  // per point: leading list entries known to lie in its component
     // one search launch per round: the points the factor keeps first, the
     // others after them (instead of a second pass)
@@ -266,10 +267,10 @@ cudaError_t proposal_trace_begin(Ctx& c);
 cudaError_t proposal_trace_end(Ctx& c);
 uint64_t splitmix(uint64_t& s);
 
-cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* kkey, uint32_t* kpos, unsigned char* kcur,
-                             int sms, cudaStream_t s);
-cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* kkey, uint32_t* kpos, unsigned char* kcur,
-                             int sms, cudaStream_t s);
+cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur, int sms,
+                             cudaStream_t s);
+cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur, int sms,
+                             cudaStream_t s);
 cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 

@@ -154,17 +154,21 @@ __device__ __forceinline__ uint64_t spread3(uint32_t x)
     return v;
 }
 
-// Hilbert index of the cell x[0..D) (bits per axis), after J. Skilling,
-// "Programming the Hilbert curve", AIP Conf. Proc. 707, 381 (2004): the
-// coordinates are turned in place into the transposed index, whose bits,
-// interleaved with axis 0 most significant in each group, form the index.
-// Cells with consecutive indices share a face, so a run of 32 consecutive
-// points has a compact bounding box; a Z-order run can jump across the
-// domain and leave a box that overlaps many others.
+// Hilbert index of the cell x[0..D) on the order-21 (3D) / order-31 (2D)
+// curve, after J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
+// 707, 381 (2004): the coordinates are turned in place into the transposed
+// index, whose bits, interleaved with axis 0 most significant in each group,
+// form the index.  Cells with consecutive indices share a face, so a run of
+// 32 consecutive points has a compact bounding box; a Z-order run can jump
+// across the domain and leave a box that overlaps many others.  The curve
+// starts at the origin and fills each origin sub-cube before leaving it, so
+// cells below 2^b on every axis get indices below 2^(D*b).
 template <int D>
-__device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3], int bits)
+__device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3])
 {
-    const uint32_t top = 1u << (bits - 1);
+    constexpr int kBits = D == 3 ? 21 : 31;
+    constexpr uint32_t top = 1u << (kBits - 1);
+#pragma unroll
     for (uint32_t q = top; q > 1; q >>= 1) {
         const uint32_t p = q - 1;
 #pragma unroll
@@ -181,6 +185,7 @@ __device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3], int bits)
 #pragma unroll
     for (int i = 1; i < D; ++i) x[i] ^= x[i - 1];  // Gray encode
     uint32_t t = 0;
+#pragma unroll
     for (uint32_t q = top; q > 1; q >>= 1)
         if (x[D - 1] & q) t ^= q - 1;
 #pragma unroll

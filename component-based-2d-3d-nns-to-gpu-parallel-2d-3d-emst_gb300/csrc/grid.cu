@@ -160,7 +160,7 @@ __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const Nor
         float qf = fminf(fmaxf(__fmul_rn(s, qs), 0.f), D == 3 ? 2097151.f : 2147483520.f);
         cell[c] = (uint32_t)qf;
     }
-    key[i] = hilbert_index<D>(cell, D == 3 ? 21 : 31);
+    key[i] = hilbert_index<D>(cell);
     idx[i] = (uint32_t)i;
 }
 
