@@ -571,14 +571,28 @@ cudaError_t cnns_select(Ctx& c)
                 if (et != cudaSuccess) return et;
             }
             if (knn && pass == 1) {  // round 1 only (decided on the device)
+                // host-driven rounds (profile mode) know the round: time the working launch
+                const bool timed = c.kernel_timer && c.round == 1;
+                if (timed) c.kernel_timer(c.timer_owner, 0, true);
                 cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream)
                                             : launch_knn_first3(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream);
                 if (ek != cudaSuccess) return ek;
+                if (timed) {
+                    c.kernel_timer(c.timer_owner, 0, false);
+                    c.knn_timed++;
+                }
                 c.launches++;
             }
+            // the component search has no work in round 1 when the lists ran
+            const bool timed = c.kernel_timer && !(knn && c.round == 1);
+            if (timed) c.kernel_timer(c.timer_owner, 1, true);
             cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
+            if (timed) {
+                c.kernel_timer(c.timer_owner, 1, false);
+                c.search_timed++;
+            }
             if (pass == 1 && !ordered && two_passes) {
                 k_filter_second<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p,
                                                                              c.lbp.p, c.ckey.p);

@@ -17,6 +17,9 @@
 #include "emst_ctx.h"
 #include "proposal.cuh"
 
+// timed phases: the operators, then the two search kernels
+enum { PH_GRID = 0, PH_OCTANTS, PH_SELECT, PH_RESOLVE, PH_HOOK, PH_FLATTEN, PH_KNN, PH_SEARCH, PH_COUNT };
+
 struct emst_ctx {
     emst::Ctx c;
     int stage = 0;  // 0: needs flatten, 1: flattened, 2: octants, 3: next-closest, 4: min-pair
@@ -30,7 +33,8 @@ struct emst_ctx {
     };
     std::vector<Pending> pending;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pool;
-    double ms[6] = {0, 0, 0, 0, 0, 0};
+    double ms[PH_COUNT] = {};
+    std::pair<cudaEvent_t, cudaEvent_t> open[2] = {};  // kernel timer: started, not yet ended
     // the whole round loop as one CUDA graph (conditional WHILE node)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -42,7 +46,23 @@ namespace {
 
 using emst::Ctx;
 
-enum { PH_GRID = 0, PH_OCTANTS, PH_SELECT, PH_RESOLVE, PH_HOOK, PH_FLATTEN };
+
+// An event pair from the context's pool (created on demand); {null, null} on failure.
+std::pair<cudaEvent_t, cudaEvent_t> take_events(emst_ctx* x)
+{
+    if (x->pool.empty()) {
+        cudaEvent_t e0, e1;
+        if (cudaEventCreate(&e0) != cudaSuccess) return {nullptr, nullptr};
+        if (cudaEventCreate(&e1) != cudaSuccess) {
+            cudaEventDestroy(e0);
+            return {nullptr, nullptr};
+        }
+        x->pool.push_back({e0, e1});
+    }
+    auto p = x->pool.back();
+    x->pool.pop_back();
+    return p;
+}
 
 // Records CUDA events around one operator on the context's stream.
 struct Timed {
@@ -52,19 +72,10 @@ struct Timed {
     Timed(emst_ctx* x_, int ph_) : x(x_), ph(ph_)
     {
         if (!x->c.profile) return;
-        if (x->pool.empty()) {
-            cudaEvent_t e0, e1;
-            if (cudaEventCreate(&e0) != cudaSuccess) return;
-            if (cudaEventCreate(&e1) != cudaSuccess) {
-                cudaEventDestroy(e0);
-                return;
-            }
-            x->pool.push_back({e0, e1});
-        }
-        a = x->pool.back().first;
-        b = x->pool.back().second;
-        x->pool.pop_back();
-        cudaEventRecord(a, x->c.stream);
+        auto p = take_events(x);
+        a = p.first;
+        b = p.second;
+        if (a) cudaEventRecord(a, x->c.stream);
     }
     ~Timed()
     {
@@ -73,6 +84,22 @@ struct Timed {
         x->pending.push_back({ph, a, b});
     }
 };
+
+// Events around one search-kernel launch (Ctx::kernel_timer): which 0 = the
+// round-1 neighbour-list kernel, 1 = the component search.
+void kernel_timer_cb(void* owner, int which, bool begin)
+{
+    emst_ctx* x = static_cast<emst_ctx*>(owner);
+    auto& o = x->open[which];
+    if (begin) {
+        o = take_events(x);
+        if (o.first) cudaEventRecord(o.first, x->c.stream);
+    } else if (o.first) {
+        cudaEventRecord(o.second, x->c.stream);
+        x->pending.push_back({PH_KNN + which, o.first, o.second});
+        o = {nullptr, nullptr};
+    }
+}
 
 // After a stream synchronisation: fold the recorded phase times in.
 void harvest(emst_ctx* x)
@@ -254,6 +281,8 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
               "counters");
     c.launches = 0;
     c.nns_launches = 0;
+    c.knn_timed = 0;
+    c.search_timed = 0;
     if (c.profile) {
         EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
         EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), c.stream), "stats");
@@ -425,6 +454,10 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
         c.first_pass_ordered = cfg->first_pass_ordered != 0;
         c.knn_seed = cfg->round1_neighbours >= 0;
+    }
+    if (c.profile) {
+        c.kernel_timer = kernel_timer_cb;
+        c.timer_owner = x;
     }
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);
@@ -685,6 +718,10 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     out->ms_resolve = x->ms[PH_RESOLVE];
     out->ms_hook = x->ms[PH_HOOK];
     out->ms_flatten = x->ms[PH_FLATTEN];
+    out->ms_knn = x->ms[PH_KNN];
+    out->ms_search = x->ms[PH_SEARCH];
+    out->knn_launches = x->c.knn_timed;
+    out->search_launches = x->c.search_timed;
     out->launches = x->c.launches;
     out->octant_launches = x->c.nns_launches;
     out->rounds = x->c.round;
@@ -829,6 +866,8 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
     EMST_CUDA(x, cudaMemcpyAsync(c.ctr.p, c.hctr, sizeof(emst::DevCounters), cudaMemcpyHostToDevice, s), "counters");
     c.launches = 0;
     c.nns_launches = 0;
+    c.knn_timed = 0;
+    c.search_timed = 0;
     for (double& v : x->ms) v = 0.0;
     if (c.profile) {
         EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");

@@ -28,6 +28,8 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/emst.h"
+
 namespace emst {
 
 // Device-side counters.  n_act / n_roots hold the CURRENT list sizes between
@@ -115,6 +117,12 @@ struct Ctx {
     // launch accounting (hand-written kernels) and optional phase timing
     int64_t launches = 0;
     int64_t nns_launches = 0;
+    // profile mode: CUDA events around the search kernels' launches (which 0:
+    // the round-1 neighbour-list kernel, 1: the component search), set by the
+    // C ABI layer; null when not profiling
+    void (*kernel_timer)(void* owner, int which, bool begin) = nullptr;
+    void* timer_owner = nullptr;
+    int64_t knn_timed = 0, search_timed = 0;  // launches timed
     bool profile = false;
     int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu)
     bool cnns_warp = false;   // component search: warp per 32 queries instead of thread per query
@@ -239,7 +247,7 @@ struct CnnsArgs {
 };
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
-constexpr int kKnn = 6;
+constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
 constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
 constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
 

@@ -44,7 +44,8 @@ class Profile(ctypes.Structure):
                 ("leaf_visits", ctypes.c_int64), ("node_tests", ctypes.c_int64), ("candidates", ctypes.c_int64),
                 ("search_warps", ctypes.c_int64), ("search_queries", ctypes.c_int64),
                 ("first_pass_searches", ctypes.c_int64), ("first_pass_resumed", ctypes.c_int64),
-                ("first_pass_deferred", ctypes.c_int64)]
+                ("first_pass_deferred", ctypes.c_int64), ("ms_knn", ctypes.c_double), ("ms_search", ctypes.c_double),
+                ("knn_launches", ctypes.c_int64), ("search_launches", ctypes.c_int64)]
 
 
 class TrainConfig(ctypes.Structure):
@@ -52,6 +53,7 @@ class TrainConfig(ctypes.Structure):
                 ("reg_weight", ctypes.c_float), ("seed", ctypes.c_uint64), ("device", ctypes.c_int)]
 
 
+ROUND1_NEIGHBOURS = 6  # EMST_ROUND1_NEIGHBOURS
 PROPOSAL_WEIGHTS = 1410
 TRACE_RECORD = 12
 

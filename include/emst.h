@@ -67,10 +67,11 @@ typedef struct {
     int first_pass_ordered; /* != 0: one search launch per round, the points
                               the factor keeps first and the others after
                               them, instead of a second pass */
-    int round1_neighbours; /* 0 = default: round 1 keeps each point's 6
-                              nearest, and later rounds take the first one
-                              outside the component without a search
-                              (6 x 12 bytes per point); -1 = off */
+    int round1_neighbours; /* 0 = default: round 1 keeps each point's
+                              EMST_ROUND1_NEIGHBOURS nearest, and later
+                              rounds take the first one outside the
+                              component without a search (8 bytes per entry
+                              + 1 per point); -1 = off */
     int reserved[1];
 } emst_config;
 
@@ -102,6 +103,14 @@ typedef struct {
     int64_t first_pass_searches;
     int64_t first_pass_resumed;
     int64_t first_pass_deferred;
+    /* component mode, profile contexts (host-driven rounds): CUDA-event time
+     * of the search kernels' own launches -- the round-1 neighbour-list
+     * kernel (its working launch) and the component search (rounds with
+     * work) -- and how many launches each figure covers */
+    double ms_knn;
+    double ms_search;
+    int64_t knn_launches;
+    int64_t search_launches;
 } emst_profile;
 
 /* Context lifetime.  Replaces CalculateurEMST::initialize / the static
@@ -283,6 +292,7 @@ emst_status emst_read_links(const char* path, int32_t* uv, int64_t cap, int64_t*
  * method's.
  * ------------------------------------------------------------------------- */
 
+#define EMST_ROUND1_NEIGHBOURS 6    /* list length of emst_config.round1_neighbours */
 #define EMST_PROPOSAL_WEIGHTS 1410 /* W1[8][32] b1[32] W2[32][32] b2[32] W3[32][2] b3[2], FP32 */
 #define EMST_TRACE_RECORD 12       /* floats per trace record */
 

@@ -2,6 +2,7 @@
 include/emst.h (no GPU needed: nothing here launches a kernel)."""
 import ctypes
 import os
+import re
 import shutil
 
 import pytest
@@ -29,6 +30,21 @@ def test_status_codes_match_header():
     txt = open(emst_gb300.HEADER).read()
     for code, name in emst_gb300.STATUS.items():
         assert ("%s = %d" % (name, code)) in txt
+
+
+def test_header_constants_match_the_binding():
+    import re
+    txt = open(emst_gb300.HEADER).read()
+    assert int(re.search(r"#define EMST_ROUND1_NEIGHBOURS (\d+)", txt).group(1)) == emst_gb300.ROUND1_NEIGHBOURS
+    assert int(re.search(r"#define EMST_PROPOSAL_WEIGHTS (\d+)", txt).group(1)) == emst_gb300.PROPOSAL_WEIGHTS
+
+
+def test_profile_struct_matches_header():
+    # the ctypes mirror has one field per emst_profile member, in order
+    txt = open(emst_gb300.HEADER).read()
+    body = txt[txt.index("typedef struct {", txt.index("ms_grid") - 200):txt.index("} emst_profile;")]
+    names = re.findall(r"^\s*(?:double|int64_t)\s+(\w+);", body, re.M)
+    assert names == [f for f, _ in emst_gb300.Profile._fields_]
 
 
 def test_null_context_is_rejected_without_touching_the_gpu():
