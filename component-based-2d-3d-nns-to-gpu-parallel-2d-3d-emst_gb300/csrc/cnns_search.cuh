@@ -2,6 +2,7 @@
 // the per-dimension translation units that instantiate it for every launch
 // shape of the table (cnns_t2.cu, cnns_t3.cu).
 #pragma once
+#include <cfloat>
 #include <climits>
 
 #include "emst_ctx.h"
@@ -335,7 +336,6 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     const uint32_t* __restrict__ perm = a.perm;
     const float4* __restrict__ nlo = a.nlo;
     const float4* __restrict__ nhi = a.nhi;
-    const uint32_t* __restrict__ nlab = a.nlab;
     const uint32_t n = a.n, L = a.L;
     const uint32_t* __restrict__ pcloud = a.pcloud;
     const uint32_t* __restrict__ ncloud = a.ncloud;
@@ -364,15 +364,19 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             kk[j] = kNoKey;
             kp[j] = kNone;
         }
-        // d2 of the K-th entry once the list is full; lanes past the list's
-        // end take -1 so that no node and no candidate is ever theirs
-        float bd = listed ? INFINITY : -1.f;
+        // d2 of the K-th entry once the list is full, FLT_MAX before (every
+        // finite bound and distance passes, an empty box's +inf does not);
+        // lanes past the list's end take -1 so that no node and no candidate
+        // is ever theirs
+        float bd = listed ? FLT_MAX : -1.f;
         uint32_t st_leaves = 0, st_nodes = 0;
 
+        // This lane's lower bound of d2 over a node's box.  An empty box
+        // (lo = +inf, hi = -inf) gives +inf through the arithmetic.  Node
+        // labels are not checked: in round 1 a node holding only the query's
+        // component holds only the query, and scanning it finds no candidate.
         auto node_lb = [&](uint32_t node) -> float {
             const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
-            if (lo.x > hi.x) return INFINITY;
-            if (__ldg(&nlab[node]) == labp) return INFINITY;
             if constexpr (CL) {
                 const uint32_t r = __ldg(&ncloud[node]);
                 if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
@@ -382,7 +386,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
             return d2_of<D>(gx, gy, gz);
         };
-        auto wanted = [&](float lb) { return lb < INFINITY && lb <= bd; };
+        auto wanted = [&](float lb) { return lb <= bd; };
         // the whole warp scans one leaf, wanted by the lanes in `need`: stage
         // it in shared memory, mark each wanting lane's points within its
         // bound, then insert each lane's marked points -- the warp runs as
