@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     // the queries: list, then (one launch, second segment) list2
     const uint32_t n1 = *n_list;
     const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
+    if (total <= a.wide_limit) return;  // a short list: k_cnns_w's (warp per query)
     for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
         const uint32_t qi = base0 + threadIdx.x;
         const bool listed = qi < total;
@@ -307,6 +308,230 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 atomicAdd(&stats[7], (unsigned long long)__popc(later));
             }
         }
+    }
+}
+
+// Component search for short query lists: one warp per query.
+//
+// With few searching points (rounds after the neighbour lists settled most of
+// them) thread-per-query warps are too few to fill the GPU and each runs 32
+// divergent traversals of dependent loads: the round waits on the slowest
+// warp.  Here a query owns a warp.  Its traversal is k_cnns_t's (own leaf,
+// then the sibling subtree of each ancestor, same bounds and pruning: the
+// query's best, its component's shared key, the per-node component labels and
+// cloud ranges), but each step tests 32 nodes at once -- the descendants
+// kWideFan levels below the popped node, one per lane -- and a leaf is scanned
+// 32 points at a time, the (d2, input id) minimum taken across the warp.
+// Leaves of a step are scanned nearest first, each re-tested against the
+// bounds; internal descendants are pushed with the nearest on top.  The
+// result, lower bound and provisional-winner record are k_cnns_t's.
+template <int D, bool CL>
+__global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
+{
+    if (a.knn_round1 && *a.round == 1) return;  // round 1 is k_knn_first's
+    const uint32_t n1 = *a.n_list;
+    const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
+    if (total > a.wide_limit) return;  // a long list: k_cnns_t's
+    const float4* __restrict__ spl = a.spl;
+    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ nlo = a.nlo;
+    const float4* __restrict__ nhi = a.nhi;
+    const uint32_t* __restrict__ nlab = a.nlab;
+    const uint32_t n = a.n, L = a.L;
+    const uint32_t* __restrict__ pcloud = a.pcloud;
+    const uint32_t* __restrict__ ncloud = a.ncloud;
+    uint64_t* __restrict__ ckey = a.ckey;
+    // stack: each step pushes at most 2^kWideFan entries and each node on the
+    // current path (at most ceil(27 / kWideFan) steps below a sibling root for
+    // 32-bit point counts) leaves at most 2^kWideFan - 1 unpopped
+    constexpr int kWStack = 256;
+    static_assert((27 + kWideFan - 1) / kWideFan * ((1 << kWideFan) - 1) + 1 <= kWStack, "traversal stack bound");
+    __shared__ uint32_t s_node[kWideWarps][kWStack];
+    __shared__ float s_lb[kWideWarps][kWStack];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t* const stack = s_node[w];
+    float* const stack_lb = s_lb[w];
+    const uint32_t below = (1u << lane) - 1u;
+    const int leaf_level = 31 - __clz(L);  // L is a power of two; node v sits on level 31 - clz(v)
+    for (uint32_t qi = blockIdx.x * kWideWarps + w; qi < total; qi += gridDim.x * kWideWarps) {
+        const uint32_t me = qi < n1 ? a.list[qi] : a.list2[qi - n1];
+        const uint32_t labp = a.lab[me];
+        const float lb0 = a.lbp[me];
+        float cb;
+        // other warps lower the key meanwhile: one lane reads it, every lane
+        // takes that value, so the warp's decisions stay uniform
+        auto refresh_cb = [&]() {
+            uint64_t k = lane == 0 ? __ldcg(&ckey[labp]) : 0ull;
+            k = __shfl_sync(kFull, k, 0);
+            cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+        };
+        refresh_cb();
+        const bool valid = !(lb0 > cb);  // else it cannot hold its component's minimum this round
+        uint32_t st_leaves = 0, st_nodes = 0;
+        bool record = false;
+        if (valid) {
+            const float4 P = spl[me];
+            const uint32_t op = __ldg(&perm[me]);
+            const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
+            float bd = INFINITY, cut = INFINITY;
+            uint64_t bkey = ~0ull;  // best: d2 bits << 32 | input id
+            uint32_t bs = kNone;     // its leaf position
+            // lower bound of d2 over a node's box, or +inf when the node
+            // cannot help (empty, all in the query's component, all in
+            // another cloud)
+            auto node_lb = [&](uint32_t node) -> float {
+                const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                if (lo.x > hi.x) return INFINITY;
+                if (__ldg(&nlab[node]) == labp) return INFINITY;
+                if constexpr (CL) {
+                    const uint32_t r = __ldg(&ncloud[node]);
+                    if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
+                }
+                const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+                const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+                return d2_of<D>(gx, gy, gz);
+            };
+            // one leaf, one point per lane; the (d2, input id) minimum across the warp
+            auto scan_leaf = [&](uint32_t leaf) {
+                const uint32_t b = leaf * 32;
+                const uint32_t m = min(32u, n - b);
+                ++st_leaves;
+                uint32_t kd = ~0u, ki = ~0u;
+                if ((uint32_t)lane < m) {
+                    const float4 c = __ldg(&spl[b + lane]);
+                    bool ok = __float_as_uint(c.w) != labp;
+                    if constexpr (CL) ok = ok && __ldg(&pcloud[b + lane]) == qc;
+                    if (ok) {
+                        kd = __float_as_uint(
+                            d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z)));
+                        ki = __ldg(&perm[b + lane]);
+                    }
+                }
+                // non-negative floats order as their bits
+                const uint32_t md = __reduce_min_sync(kFull, kd);
+                const uint32_t mi = __reduce_min_sync(kFull, kd == md ? ki : ~0u);
+                const uint64_t mk = ((uint64_t)md << 32) | mi;
+                if (mk < bkey) {
+                    const uint32_t src = __ffs(__ballot_sync(kFull, kd == md && ki == mi)) - 1;
+                    bkey = mk;
+                    bd = __uint_as_float(md);
+                    bs = b + src;
+                }
+                refresh_cb();
+            };
+
+            const uint32_t own = me >> 5;
+            if (__ldg(&nlab[L + own]) != labp) scan_leaf(own);
+            for (uint32_t v = L + own; v > 1; v >>= 1) {
+                const uint32_t sib = v ^ 1u;
+                ++st_nodes;
+                const float ls = node_lb(sib);
+                if (!(ls < INFINITY) || ls > bd) continue;
+                if (ls > cb) {  // ruled out by the component's key only: bounds this point's distance
+                    cut = fminf(cut, ls);
+                    continue;
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    stack[0] = sib;
+                    stack_lb[0] = ls;
+                }
+                int top = 1;
+                __syncwarp();
+                while (top > 0) {
+                    --top;
+                    const uint32_t node = stack[top];
+                    const float lnode = stack_lb[top];
+                    // bounds re-checked: they may have shrunk since the push
+                    if (lnode > bd) continue;
+                    if (lnode > cb) {
+                        cut = fminf(cut, lnode);
+                        continue;
+                    }
+                    const int lev = leaf_level - (31 - __clz(node));  // levels down to the leaves
+                    const int e = min(lev, kWideFan);
+                    const uint32_t cnt = 1u << e;
+                    const uint32_t d = (node << e) + (uint32_t)lane;
+                    const float lb = (uint32_t)lane < cnt ? node_lb(d) : INFINITY;
+                    st_nodes += cnt;
+                    {
+                        // descendants only the component's key rules out bound the distance
+                        const float lim = fminf(bd, cb);
+                        const bool cutc = lb < INFINITY && lb > lim && lb <= bd;
+                        cut = fminf(cut, __uint_as_float(
+                                             __reduce_min_sync(kFull, cutc ? __float_as_uint(lb) : 0x7f800000u)));
+                    }
+                    uint32_t want = __ballot_sync(kFull, lb < INFINITY && lb <= fminf(bd, cb));
+                    if (e == lev) {
+                        // leaves, nearest first, each against the current bounds
+                        while (want) {
+                            const uint32_t mlb =
+                                __reduce_min_sync(kFull, (want >> lane & 1u) ? __float_as_uint(lb) : ~0u);
+                            const int j =
+                                __ffs(__ballot_sync(kFull, (want >> lane & 1u) && __float_as_uint(lb) == mlb)) - 1;
+                            want &= ~(1u << j);
+                            const float lj = __uint_as_float(mlb);
+                            if (lj > bd) break;  // this and the rest: farther than the best
+                            if (lj > cb) {       // this and the rest: ruled out by the component's key only
+                                cut = fminf(cut, lj);
+                                break;
+                            }
+                            scan_leaf((node << e) + (uint32_t)j - L);
+                        }
+                    } else if (want) {
+                        // internal descendants: the nearest pushed last, searched next
+                        const uint32_t mlb = __reduce_min_sync(kFull, (want >> lane & 1u) ? __float_as_uint(lb) : ~0u);
+                        const int jn =
+                            __ffs(__ballot_sync(kFull, (want >> lane & 1u) && __float_as_uint(lb) == mlb)) - 1;
+                        const uint32_t rest = want & ~(1u << jn);
+                        const int nr = __popc(rest);
+                        if (top + nr + 1 > kWStack) break;  // unreachable: see kWStack
+                        __syncwarp();  // every lane has read the popped entry
+                        if (rest >> lane & 1u) {
+                            const int at = top + __popc(rest & below);
+                            stack[at] = d;
+                            stack_lb[at] = lb;
+                        }
+                        if (lane == jn) {
+                            stack[top + nr] = d;
+                            stack_lb[top + nr] = lb;
+                        }
+                        top += nr + 1;
+                        __syncwarp();
+                    }
+                }
+            }
+            const bool exact = bs != kNone && bd < cut;
+            if (lane == 0) {
+                a.lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
+                if (bs != kNone) {
+                    const uint32_t mn = min(op, (uint32_t)bkey);
+                    const uint64_t key = (bkey & 0xffffffff00000000ull) | mn;
+                    a.selq[me] = exact ? bs : kNone;
+                    a.selkey[me] = key;
+                    if (key <= __ldcg(&ckey[labp])) {
+                        const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
+                        record = old >= key;
+                    }
+                } else {
+                    a.selq[me] = kNone;
+                }
+            }
+        }
+        if (lane == 0) {
+            if (a.pass == 1) a.dflag[me] = 0;
+            if (record) a.prov[atomicAdd(a.n_prov, 1u)] = me;
+            if (a.stats) {
+                atomicAdd(&a.stats[0], (unsigned long long)st_leaves);
+                atomicAdd(&a.stats[1], (unsigned long long)st_nodes);
+                atomicAdd(&a.stats[2], (unsigned long long)st_leaves * 32ull);
+                atomicAdd(&a.stats[3], 1ull);
+                atomicAdd(&a.stats[4], valid ? 1ull : 0ull);
+                atomicAdd(&a.stats[5], valid && a.pass == 1 ? 1ull : 0ull);
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -584,6 +809,14 @@ cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
     case 4: launch_shape<D, CL, 4, LEARN>(a, sms, s); break;
     case 5: launch_shape<D, CL, 5, LEARN>(a, sms, s); break;
     default: return cudaErrorInvalidValue;
+    }
+    if (a.wide_limit > 0 && !LEARN) {
+        // the warp-per-query kernel for short lists (each kernel reads the
+        // list's length on the device and leaves the other's lists alone)
+        uint64_t b = ((uint64_t)a.wide_limit + kWideWarps - 1) / kWideWarps;
+        const uint64_t cap = (uint64_t)sms * 16;
+        if (b > cap) b = cap;
+        k_cnns_w<D, CL><<<(unsigned)b, kWideWarps * 32, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

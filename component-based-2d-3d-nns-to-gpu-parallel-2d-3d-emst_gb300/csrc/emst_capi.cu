@@ -454,6 +454,7 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
         c.first_pass_ordered = cfg->first_pass_ordered != 0;
         c.knn_seed = cfg->round1_neighbours >= 0;
+        c.wide_search = cfg->wide_search >= 0;
     }
     if (c.profile) {
         c.kernel_timer = kernel_timer_cb;

@@ -158,6 +158,8 @@ struct Ctx {
     // round 1 keeps each point's kKnn nearest (k_knn_first); later rounds take
     // the first entry outside the component without a search (k_reuse)
     bool knn_seed = true;
+    // short query lists searched one warp per query (k_cnns_w)
+    bool wide_search = true;
     // kKnn entries per point, entry-major (entry j of point p at j * n + p):
     // d2 bits << 32 | leaf position, sorted by (d2, input id); ~0 = no entry
     DevBuf<uint64_t> klist;
@@ -244,12 +246,18 @@ struct CnnsArgs {
     const uint32_t* list2;    // second segment of the same launch (ordered first pass), or null
     const uint32_t* n_list2;
     bool knn_round1;          // round 1 runs k_knn_first (neighbour lists), not this kernel
+    // lists of at most this many queries go to k_cnns_w (warp per query), longer
+    // ones to k_cnns_t (thread per query); 0: k_cnns_t only
+    uint32_t wide_limit;
 };
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
 constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
 constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
-constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
+constexpr int kKnnDense = 16;
+constexpr int kWideWarps = 8;         // warps per block of k_cnns_w
+constexpr int kWideFan = 5;           // k_cnns_w: levels a traversal step descends (32 nodes, one per lane)
+constexpr uint32_t kWideLimit = 65536;   // longest query list k_cnns_w takes (warp per query)  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the

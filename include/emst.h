@@ -72,7 +72,10 @@ typedef struct {
                               rounds take the first one outside the
                               component without a search (8 bytes per entry
                               + 1 per point); -1 = off */
-    int reserved[1];
+    int wide_search;       /* 0 = default: a search round whose query list
+                              holds at most 65536 points runs one warp per
+                              query (k_cnns_w), longer lists one thread per
+                              query (k_cnns_t); -1 = thread per query only */
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel

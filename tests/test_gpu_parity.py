@@ -233,7 +233,8 @@ def test_every_search_shape_same_edges(gpu_lib, kind, dim, n):
     count, threads, min_blocks = gpu_lib.search_shapes()
     assert count >= 2 and all(t % 32 == 0 for t in threads) and all(m >= 1 for m in min_blocks)
     for k in range(1, count + 1):
-        with gpu_lib.Emst(search_shape=k) as e:
+        # thread per query for every list, so each shape of k_cnns_t runs
+        with gpu_lib.Emst(search_shape=k, wide_search=-1) as e:
             assert e.search_shape() == k
             uv, ln = e.solve(pts)
             assert np.array_equal(_canon(uv), _canon(ref)), k
@@ -301,14 +302,16 @@ def test_device_outputs_ordered_on_caller_stream(gpu_lib, which):
                                 dict(first_pass_factor=1.5, first_pass_ordered=True),
                                 dict(first_pass_factor=float("inf"), first_pass_ordered=True)])
 @pytest.mark.parametrize("kind,dim", [("cluster", 3), ("dups", 2), ("lattice", 3)])
-def test_first_pass_rules_keep_edges(gpu_lib, kw, kind, dim):
+@pytest.mark.parametrize("wide", [0, -1])
+def test_first_pass_rules_keep_edges(gpu_lib, kw, kind, dim, wide):
     """The first-pass rule (who searches first, in one launch or two) only
-    changes the order of the searches, never the edge set."""
+    changes the order of the searches, never the edge set -- with short
+    lists searched warp per query or thread per query."""
     pts = family(kind, 20000, dim, 71)
     with gpu_lib.Emst() as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
-    with gpu_lib.Emst(**kw) as e:
+    with gpu_lib.Emst(wide_search=wide, **kw) as e:
         uv, ln = e.solve(pts)
         assert np.array_equal(_canon(uv), _canon(ref))
         assert ln == pytest.approx(ref_len, rel=1e-12)
@@ -451,3 +454,29 @@ def test_full_size_structure(gpu_lib, name, n):
     assert np.array_equal(_canon(uv0), _canon(uv))
     for k in range(1, int(r1.max()) + 1):
         assert np.array_equal(_canon(uv0[r0 == k]), _canon(uv1[r1 == k]))
+
+
+@pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 40000), ("uniform", 2, 40000), ("dups", 3, 8000),
+                                        ("lattice", 2, 6000), ("line", 3, 3000), ("dups", 2, 9),
+                                        ("cluster", 2, 150000)])
+def test_warp_per_query_search_keeps_edges(gpu_lib, kind, dim, n):
+    """Short query lists searched one warp per query (k_cnns_w, default) give
+    the thread-per-query search's edges, lengths and per-round edge counts, in
+    the graph loop, the host loop and batches; without neighbour lists too."""
+    pts = family(kind, n, dim, 97)
+    with gpu_lib.Emst(wide_search=-1) as e:
+        ref, ref_len = e.solve(pts)
+        ref_rounds = e.round_stats()
+    for kw in (dict(), dict(host_rounds=True), dict(round1_neighbours=-1)):
+        with gpu_lib.Emst(**kw) as e:
+            uv, ln = e.solve(pts)
+            assert np.array_equal(_canon(uv), _canon(ref)), kw
+            assert ln == pytest.approx(ref_len, rel=1e-12)
+            assert np.array_equal(e.round_stats(), ref_rounds), kw
+    other = family("uniform", max(n // 3, 2), dim, 98)
+    with gpu_lib.Emst(wide_search=-1) as e:
+        ref_b, _ = e.solve_batch([pts, other])
+    with gpu_lib.Emst() as e:
+        got_b, _ = e.solve_batch([pts, other])
+    for a, b in zip(ref_b, got_b):
+        assert np.array_equal(_canon(a), _canon(b))
