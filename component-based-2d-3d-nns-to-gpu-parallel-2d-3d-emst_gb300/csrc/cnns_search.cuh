@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     const uint32_t n1 = *n_list;
     const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
     if (total <= a.wide_limit) return;  // a short list: k_cnns_w's (warp per query)
+    if (total > a.coop_min) return;     // a long list: k_cnns_c's (warp per 32 queries, walking together)
     for (uint32_t base0 = blockIdx.x * blockDim.x; base0 < total; base0 += gridDim.x * blockDim.x) {
         const uint32_t qi = base0 + threadIdx.x;
         const bool listed = qi < total;
@@ -535,6 +536,240 @@ __global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
     }
 }
 
+// Component search for long query lists: one warp per 32 consecutive
+// queries, walking the tree together (k_knn_first's traversal), each lane
+// keeping its own nearest point outside its component.
+//
+// In late rounds most points of most leaves search, so a warp's 32 queries
+// are a leaf's points, in one component, and their bottom-up walks visit the
+// same nodes; thread per query runs those walks as 32 divergent copies.  Per
+// lane this is k_cnns_t's search: the bound is the lane's best and its
+// component's key, nodes holding only its component or only other clouds are
+// skipped, and nodes only the component's key rules out bound its distance
+// from below (cut).  A node is entered when any lane wants it, so a lane may
+// test points beyond its bound: those only lower its best to a real
+// candidate, never past its true nearest.  A lane adds a node's bound to its
+// cut whenever the key rules the node out for it, even if the warp enters the
+// node for another lane: cut stays a lower bound of every point it skipped,
+// so a result it calls exact is exact.
+template <int D, bool CL>
+__global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
+{
+    if (a.knn_round1 && *a.round == 1) return;  // round 1 is k_knn_first's
+    const uint32_t n1 = *a.n_list;
+    const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
+    if (total <= a.wide_limit || total <= a.coop_min) return;  // shorter lists: k_cnns_w, k_cnns_t
+    const float4* __restrict__ spl = a.spl;
+    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ nlo = a.nlo;
+    const float4* __restrict__ nhi = a.nhi;
+    const uint32_t* __restrict__ nlab = a.nlab;
+    const uint32_t n = a.n, L = a.L;
+    const uint32_t* __restrict__ pcloud = a.pcloud;
+    const uint32_t* __restrict__ ncloud = a.ncloud;
+    uint64_t* __restrict__ ckey = a.ckey;
+    constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
+    __shared__ float4 s_pt[kKnnWarps][32];
+    __shared__ uint32_t s_id[kKnnWarps][32];
+    __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
+    __shared__ uint32_t s_stack[kKnnWarps][kWStack];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* const pt = s_pt[w];
+    uint32_t* const ids = s_id[w];
+    uint32_t* const stack = s_stack[w];
+    const uint32_t stride = gridDim.x * kKnnWarps * 32;
+    for (uint32_t base0 = (blockIdx.x * kKnnWarps + w) * 32; base0 < total; base0 += stride) {
+        const uint32_t qi = base0 + lane;
+        const bool listed = qi < total;
+        const uint32_t qs = listed ? qi : base0;
+        const uint32_t me = qs < n1 ? a.list[qs] : a.list2[qs - n1];
+        const uint32_t labp = listed ? a.lab[me] : kEmpty;
+        const float lb0 = listed ? a.lbp[me] : 0.f;
+        float cb = INFINITY;
+        auto refresh_cb = [&]() {
+            if (listed) {
+                const uint64_t k = __ldcg(&ckey[labp]);
+                cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
+            }
+        };
+        refresh_cb();
+        const bool valid = listed && !(lb0 > cb);  // else it cannot hold its component's minimum this round
+        const float4 P = spl[me];
+        const uint32_t op = __ldg(&perm[me]);
+        const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
+        // best d2 so far (+inf: none); -1 for lanes with no search, so that
+        // no node and no candidate is ever theirs
+        float bd = valid ? INFINITY : -1.f;
+        float cut = INFINITY;
+        uint32_t bo = ~0u, bs = kNone;  // best's input id and leaf position
+        uint32_t st_leaves = 0, st_nodes = 0;
+
+        // this lane's lower bound of d2 over a node's box, or +inf when the
+        // node cannot help it (empty, all in its component, all in other clouds)
+        auto node_lb = [&](uint32_t node) -> float {
+            const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+            if (__ldg(&nlab[node]) == labp) return INFINITY;
+            if constexpr (CL) {
+                const uint32_t r = __ldg(&ncloud[node]);
+                if (qc < (r >> 16) || qc > (r & 0xffffu)) return INFINITY;
+            }
+            const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, P.x), __fsub_rn(P.x, hi.x)), 0.f);
+            const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, P.y), __fsub_rn(P.y, hi.y)), 0.f);
+            const float gz = D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, P.z), __fsub_rn(P.z, hi.z)), 0.f) : 0.f;
+            return d2_of<D>(gx, gy, gz);
+        };
+        auto wanted = [&](float lb) { return lb < INFINITY && lb <= fminf(bd, cb); };
+        // a node the component's key (not the best) rules out bounds the distance
+        auto note = [&](float lb) {
+            if (lb < INFINITY && lb > fminf(bd, cb) && lb <= bd) cut = fminf(cut, lb);
+        };
+        // the whole warp scans one leaf for the lanes in `need` (as
+        // k_knn_first: staged in shared memory; every lane tests all points
+        // when many lanes want the leaf, else one ballot-free minimum per
+        // wanting lane), each lane keeping its (d2, input id) minimum
+        auto scan_leaf = [&](uint32_t leaf, uint32_t need) {
+            const uint32_t b = leaf * 32;
+            const uint32_t m = min(32u, n - b);
+            ++st_leaves;
+            __syncwarp();  // the previous leaf's reads are done
+            if ((uint32_t)lane < m) {
+                pt[lane] = __ldg(&spl[b + lane]);
+                ids[lane] = __ldg(&perm[b + lane]);
+                if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
+            } else {
+                // past the last point: NaN coordinates fail every d2 <= bound test
+                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(kEmpty));
+                ids[lane] = ~0u;
+                if constexpr (CL) s_cl[w][lane] = ~0u;
+            }
+            __syncwarp();
+            if (__popc(need) > kKnnDense) {
+#pragma unroll 8
+                for (int j = 0; j < 32; ++j) {
+                    const float4 c = pt[j];
+                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                    bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
+                    if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                    const uint32_t id = ids[j];
+                    const bool better = ok && (d2 < bd || id < bo);  // (d2, id) order; ok has d2 <= bd
+                    bd = better ? d2 : bd;
+                    bo = better ? id : bo;
+                    bs = better ? b + (uint32_t)j : bs;
+                }
+            } else {
+                const float4 c = pt[lane];
+                const uint32_t cid = ids[lane];
+                const uint32_t cc = CL ? s_cl[w][lane] : 0u;
+                while (need) {
+                    const int q = __ffs(need) - 1;
+                    need &= need - 1u;
+                    // every lane takes part in every shuffle and reduction
+                    const float qx = __shfl_sync(kFull, P.x, q), qy = __shfl_sync(kFull, P.y, q);
+                    const float qz = D == 3 ? __shfl_sync(kFull, P.z, q) : 0.f;
+                    const float qb = __shfl_sync(kFull, bd, q);
+                    const uint32_t ql = __shfl_sync(kFull, labp, q);
+                    const uint32_t qq = CL ? __shfl_sync(kFull, qc, q) : 0u;
+                    const float d2 = d2_of<D>(__fsub_rn(c.x, qx), __fsub_rn(c.y, qy), __fsub_rn(c.z, qz));
+                    bool ok = d2 <= qb && __float_as_uint(c.w) != ql;
+                    if constexpr (CL) ok = ok && cc == qq;
+                    const uint32_t kd = ok ? __float_as_uint(d2) : ~0u;  // non-negative floats order as bits
+                    const uint32_t md = __reduce_min_sync(kFull, kd);
+                    const uint32_t mi = __reduce_min_sync(kFull, kd == md ? cid : ~0u);
+                    const uint32_t src = __ffs(__ballot_sync(kFull, kd == md && cid == mi)) - 1;
+                    if (lane == q && md != ~0u) {
+                        const float d = __uint_as_float(md);
+                        if (d < bd || mi < bo) {
+                            bd = d;
+                            bo = mi;
+                            bs = b + src;
+                        }
+                    }
+                }
+            }
+            refresh_cb();
+        };
+
+        // the warp's own leaf (lane 0's query's) first, then bottom-up: every
+        // other leaf lies in exactly one sibling subtree of its ancestors
+        const uint32_t own = __shfl_sync(kFull, me, 0) >> 5;
+        {
+            const float lo = node_lb(L + own);
+            note(lo);
+            const uint32_t need = __ballot_sync(kFull, wanted(lo));
+            if (need) scan_leaf(own, need);
+        }
+        for (uint32_t v = L + own; v > 1; v >>= 1) {
+            const uint32_t sib = v ^ 1u;
+            ++st_nodes;
+            {
+                const float ls = node_lb(sib);
+                note(ls);
+                if (!__any_sync(kFull, wanted(ls))) continue;
+            }
+            int top = 0;
+            stack[top++] = sib;
+            while (top > 0) {
+                const uint32_t node = stack[--top];
+                ++st_nodes;
+                if (node >= L) {
+                    // bounds re-checked: they may have shrunk since the push
+                    const float lb = node_lb(node);
+                    note(lb);
+                    const uint32_t need = __ballot_sync(kFull, wanted(lb));
+                    if (need) scan_leaf(node - L, need);
+                    continue;
+                }
+                const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                const float l0 = node_lb(c0), l1 = node_lb(c1);
+                note(l0);
+                note(l1);
+                const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
+                // the child nearer to the warp's nearest lane is searched next
+                const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
+                const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
+                const bool near0 = m0 <= m1;
+                const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
+                __syncwarp();  // every lane has read the popped entry
+                if (wf) stack[top++] = near0 ? c1 : c0;
+                if (wn) stack[top++] = near0 ? c0 : c1;
+                __syncwarp();
+            }
+        }
+        bool record = false;
+        if (valid) {
+            const bool exact = bs != kNone && bd < cut;
+            a.lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
+            if (bs != kNone) {
+                const uint32_t mn = min(op, bo);
+                const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
+                a.selq[me] = exact ? bs : kNone;
+                a.selkey[me] = key;
+                if (key <= __ldcg(&ckey[labp])) {
+                    const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
+                    record = old >= key;
+                }
+            } else {
+                a.selq[me] = kNone;
+            }
+        }
+        if (listed && a.pass == 1) a.dflag[me] = 0;
+        __syncwarp();
+        warp_append(record, me, a.prov, a.n_prov);
+        if (a.stats) {
+            const uint32_t q = __popc(__ballot_sync(kFull, valid));
+            const uint32_t f = __popc(__ballot_sync(kFull, valid && a.pass == 1));
+            if (lane == 0) {
+                atomicAdd(&a.stats[0], (unsigned long long)st_leaves);
+                atomicAdd(&a.stats[1], (unsigned long long)st_nodes * 2ull * q);
+                atomicAdd(&a.stats[2], (unsigned long long)st_leaves * 32ull * q);
+                atomicAdd(&a.stats[3], 1ull);
+                atomicAdd(&a.stats[4], (unsigned long long)q);
+                atomicAdd(&a.stats[5], (unsigned long long)f);
+            }
+        }
+    }
+}
+
 // Round 1 with neighbour lists: each point's kKnn nearest other points (its
 // component is itself), sorted by (d2, input id) and kept for later rounds:
 // there, the first entry outside the point's component is its exact nearest
@@ -817,6 +1052,15 @@ cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
         const uint64_t cap = (uint64_t)sms * 16;
         if (b > cap) b = cap;
         k_cnns_w<D, CL><<<(unsigned)b, kWideWarps * 32, 0, s>>>(a);
+    }
+    if (a.coop_min != kNoCoop && !LEARN) {
+        // the cooperative kernel for long lists (grid: as k_knn_first's)
+        constexpr int T = kKnnWarps * 32;
+        uint64_t b = ((uint64_t)a.n + T - 1) / T;
+        const uint64_t cap = (uint64_t)sms * 4 * 4;
+        if (b > cap) b = cap;
+        if (b < 1) b = 1;
+        k_cnns_c<D, CL><<<(unsigned)b, T, 0, s>>>(a);
     }
     return cudaGetLastError();
 }

@@ -454,7 +454,11 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
         c.first_pass_ordered = cfg->first_pass_ordered != 0;
         c.knn_seed = cfg->round1_neighbours >= 0;
-        c.wide_search = cfg->wide_search >= 0;
+        if (cfg->wide_search < -1 || cfg->wide_search > 2) {
+            delete x;
+            return EMST_EINVAL;
+        }
+        c.search_split = cfg->wide_search;
     }
     if (c.profile) {
         c.kernel_timer = kernel_timer_cb;

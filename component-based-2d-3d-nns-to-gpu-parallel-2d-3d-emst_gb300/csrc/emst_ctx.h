@@ -158,8 +158,10 @@ struct Ctx {
     // round 1 keeps each point's kKnn nearest (k_knn_first); later rounds take
     // the first entry outside the component without a search (k_reuse)
     bool knn_seed = true;
-    // short query lists searched one warp per query (k_cnns_w)
-    bool wide_search = true;
+    // which kernel searches a round's query list: 0 by its length (k_cnns_w
+    // for short lists, k_cnns_c for long ones, k_cnns_t between), -1 k_cnns_t
+    // only, 1 k_cnns_w only, 2 k_cnns_c only
+    int search_split = 0;
     // kKnn entries per point, entry-major (entry j of point p at j * n + p):
     // d2 bits << 32 | leaf position, sorted by (d2, input id); ~0 = no entry
     DevBuf<uint64_t> klist;
@@ -249,6 +251,9 @@ struct CnnsArgs {
     // lists of at most this many queries go to k_cnns_w (warp per query), longer
     // ones to k_cnns_t (thread per query); 0: k_cnns_t only
     uint32_t wide_limit;
+    // lists longer than this (and than wide_limit) go to k_cnns_c (warp per
+    // 32 queries walking together); kNoCoop: never
+    uint32_t coop_min;
 };
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
@@ -261,6 +266,10 @@ constexpr int kWideFan = 5;    // k_cnns_w: levels a traversal step descends (32
 // thread per query (k_cnns_t).  Measured at 10^7 points: 5.6k queries 0.06 vs
 // 0.41 ms, 94k queries 0.42 vs 0.37 ms
 constexpr uint32_t kWideLimit = 65536;
+// shortest query list k_cnns_c takes: late rounds where most points of most
+// leaves search, so a warp's 32 queries walk the same nodes
+constexpr uint32_t kCoopMin = 1000000;
+constexpr uint32_t kNoCoop = 0xffffffffu;
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the

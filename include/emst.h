@@ -72,10 +72,15 @@ typedef struct {
                               rounds take the first one outside the
                               component without a search (8 bytes per entry
                               + 1 per point); -1 = off */
-    int wide_search;       /* 0 = default: a search round whose query list
-                              holds at most 65536 points runs one warp per
-                              query (k_cnns_w), longer lists one thread per
-                              query (k_cnns_t); -1 = thread per query only */
+    int wide_search;       /* which kernel searches a round's query list:
+                              0 = default, by its length: at most 65536
+                              points one warp per query (k_cnns_w), more than
+                              10^6 one warp per 32 queries walking the tree
+                              together (k_cnns_c), one thread per query
+                              between (k_cnns_t); -1 = thread per query
+                              only; 1 = warp per query only; 2 = warp per 32
+                              queries only.  Every choice gives the same
+                              edges; other values: EMST_EINVAL */
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel

@@ -459,16 +459,19 @@ def test_full_size_structure(gpu_lib, name, n):
 @pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 40000), ("uniform", 2, 40000), ("dups", 3, 8000),
                                         ("lattice", 2, 6000), ("line", 3, 3000), ("dups", 2, 9),
                                         ("cluster", 2, 150000)])
-def test_warp_per_query_search_keeps_edges(gpu_lib, kind, dim, n):
-    """Short query lists searched one warp per query (k_cnns_w, default) give
-    the thread-per-query search's edges, lengths and per-round edge counts, in
-    the graph loop, the host loop and batches; without neighbour lists too."""
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_search_kernels_keep_edges(gpu_lib, kind, dim, n, mode):
+    """Every search kernel gives the thread-per-query search's edges, lengths
+    and per-round edge counts, in the graph loop, the host loop and batches,
+    without neighbour lists too: the default split by list length (0), warp
+    per query for every list (1, k_cnns_w), warp per 32 queries walking the
+    tree together for every list (2, k_cnns_c)."""
     pts = family(kind, n, dim, 97)
     with gpu_lib.Emst(wide_search=-1) as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
     for kw in (dict(), dict(host_rounds=True), dict(round1_neighbours=-1)):
-        with gpu_lib.Emst(**kw) as e:
+        with gpu_lib.Emst(wide_search=mode, **kw) as e:
             uv, ln = e.solve(pts)
             assert np.array_equal(_canon(uv), _canon(ref)), kw
             assert ln == pytest.approx(ref_len, rel=1e-12)
@@ -476,7 +479,13 @@ def test_warp_per_query_search_keeps_edges(gpu_lib, kind, dim, n):
     other = family("uniform", max(n // 3, 2), dim, 98)
     with gpu_lib.Emst(wide_search=-1) as e:
         ref_b, _ = e.solve_batch([pts, other])
-    with gpu_lib.Emst() as e:
+    with gpu_lib.Emst(wide_search=mode) as e:
         got_b, _ = e.solve_batch([pts, other])
     for a, b in zip(ref_b, got_b):
         assert np.array_equal(_canon(a), _canon(b))
+
+
+def test_search_split_rejects_unknown_values(gpu_lib):
+    for bad in (-2, 3):
+        with pytest.raises(gpu_lib.EmstError):
+            gpu_lib.Emst(wide_search=bad)
