@@ -558,16 +558,16 @@ cudaError_t cnns_select(Ctx& c)
                        cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
                        c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
                        c.threshold, &d->round,   nullptr,  nullptr,   knn};
-            // the learned first pass runs its inference in k_cnns_t: it keeps every list
+            // the learned first pass steers the lists k_cnns_t takes (its
+            // inference runs there); the other kernels search theirs plainly
+            // and defer nothing
             a.wide_limit = 0u;
             a.coop_min = kNoCoop;
-            if (!(c.learned && pass == 1 && !pc)) {
-                switch (c.search_split) {
-                case 0: a.wide_limit = kWideLimit; a.coop_min = kCoopMin; break;
-                case 1: a.wide_limit = 0xffffffffu; break;
-                case 2: a.coop_min = 0u; break;
-                default: break;
-                }
+            switch (c.search_split) {
+            case 0: a.wide_limit = kWideLimit; a.coop_min = kCoopMin; break;
+            case 1: a.wide_limit = 0xffffffffu; break;
+            case 2: a.coop_min = 0u; break;
+            default: break;
             }
             const bool ordered = c.first_pass_ordered && !(c.learned && !pc);
             if (ordered) {  // both segments in this one launch; no second pass
@@ -600,8 +600,8 @@ cudaError_t cnns_select(Ctx& c)
             cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
                                         : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
-            if (a.wide_limit > 0 && !learned) c.launches++;         // k_cnns_w beside k_cnns_t
-            if (a.coop_min != kNoCoop && !learned) c.launches++;  // k_cnns_c beside them
+            if (a.wide_limit > 0) c.launches++;         // k_cnns_w beside k_cnns_t
+            if (a.coop_min != kNoCoop) c.launches++;  // k_cnns_c beside them
             if (timed) {
                 c.kernel_timer(c.timer_owner, 1, false);
                 c.search_timed++;

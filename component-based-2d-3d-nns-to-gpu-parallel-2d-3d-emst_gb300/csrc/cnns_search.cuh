@@ -1045,7 +1045,7 @@ cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
     case 5: launch_shape<D, CL, 5, LEARN>(a, sms, s); break;
     default: return cudaErrorInvalidValue;
     }
-    if (a.wide_limit > 0 && !LEARN) {
+    if (a.wide_limit > 0) {
         // the warp-per-query kernel for short lists (each kernel reads the
         // list's length on the device and leaves the other's lists alone)
         uint64_t b = ((uint64_t)a.wide_limit + kWideWarps - 1) / kWideWarps;
@@ -1053,7 +1053,7 @@ cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
         if (b > cap) b = cap;
         k_cnns_w<D, CL><<<(unsigned)b, kWideWarps * 32, 0, s>>>(a);
     }
-    if (a.coop_min != kNoCoop && !LEARN) {
+    if (a.coop_min != kNoCoop) {
         // the cooperative kernel for long lists (grid: as k_knn_first's)
         constexpr int T = kKnnWarps * 32;
         uint64_t b = ((uint64_t)a.n + T - 1) / T;

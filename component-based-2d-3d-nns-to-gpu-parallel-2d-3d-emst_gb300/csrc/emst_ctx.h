@@ -266,9 +266,11 @@ constexpr int kWideFan = 5;    // k_cnns_w: levels a traversal step descends (32
 // thread per query (k_cnns_t).  Measured at 10^7 points: 5.6k queries 0.06 vs
 // 0.41 ms, 94k queries 0.42 vs 0.37 ms
 constexpr uint32_t kWideLimit = 65536;
-// shortest query list k_cnns_c takes: late rounds where most points of most
-// leaves search, so a warp's 32 queries walk the same nodes
-constexpr uint32_t kCoopMin = 1000000;
+// shortest query list k_cnns_c takes: rounds where enough points of a leaf
+// search that a warp's 32 queries walk mostly the same nodes.  Swept (profile
+// solves of gauss3d_1e7 / bezier2d_1e7): 150k 18.30 / 13.37 ms, 400k 18.50 /
+// 13.43, 10^6 18.57 / 13.51
+constexpr uint32_t kCoopMin = 150000;
 constexpr uint32_t kNoCoop = 0xffffffffu;
 
 // Launch shapes of the component search: threads per block and the minimum

@@ -100,13 +100,16 @@ def test_learned_first_pass_keeps_edges_and_rounds(gpu_lib, kind, dim, n):
     with gpu_lib.Emst() as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
-    for name, w, margin in _weight_sets(gpu_lib):
-        with gpu_lib.Emst() as e:
-            e.set_proposal(w, margin)
-            uv, ln = e.solve(pts)
-            assert np.array_equal(_canon(uv), _canon(ref)), name
-            assert ln == pytest.approx(ref_len, rel=1e-12), name
-            assert np.array_equal(e.round_stats(), ref_rounds), name
+    # wide_search -1: every list through the learned thread-per-query pass;
+    # 0: the default split, the learned pass steering the mid-length lists
+    for wide in (-1, 0):
+        for name, w, margin in _weight_sets(gpu_lib):
+            with gpu_lib.Emst(wide_search=wide) as e:
+                e.set_proposal(w, margin)
+                uv, ln = e.solve(pts)
+                assert np.array_equal(_canon(uv), _canon(ref)), (wide, name)
+                assert ln == pytest.approx(ref_len, rel=1e-12), (wide, name)
+                assert np.array_equal(e.round_stats(), ref_rounds), (wide, name)
 
 
 def test_learned_graph_and_host_loops_agree(gpu_lib):
@@ -114,12 +117,14 @@ def test_learned_graph_and_host_loops_agree(gpu_lib):
     w = gpu_lib.proposal_init(9)
     out = []
     for host in (False, True):
-        with gpu_lib.Emst(host_rounds=host) as e:
-            e.set_proposal(w, 1.0)
-            out.append(_canon(e.solve(pts)[0]))
+        for wide in (-1, 0):
+            with gpu_lib.Emst(host_rounds=host, wide_search=wide) as e:
+                e.set_proposal(w, 1.0)
+                out.append(_canon(e.solve(pts)[0]))
     with gpu_lib.Emst() as e:
         ref = _canon(e.solve(pts)[0])
-    assert np.array_equal(out[0], ref) and np.array_equal(out[1], ref)
+    for got in out:
+        assert np.array_equal(got, ref)
 
 
 def test_first_pass_counters(gpu_lib):
