@@ -75,7 +75,7 @@ typedef struct {
     int wide_search;       /* which kernel searches a round's query list:
                               0 = default, by its length: at most 65536
                               points one warp per query (k_cnns_w), more than
-                              10^6 one warp per 32 queries walking the tree
+                              150000 one warp per 32 queries walking the tree
                               together (k_cnns_c), one thread per query
                               between (k_cnns_t); -1 = thread per query
                               only; 1 = warp per query only; 2 = warp per 32
