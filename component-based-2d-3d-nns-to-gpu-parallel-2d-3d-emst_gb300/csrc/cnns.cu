@@ -343,15 +343,14 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 }
 
-// Per round: points in leaf order with their current component label.
-__global__ void k_pack_spl(uint32_t n, const float4* __restrict__ sp, const uint32_t* __restrict__ lab,
-                           float4* __restrict__ spl)
+// Per round: each point's current component label into the .w word of its
+// packed (x, y, z, label) record.  The coordinates are copied once per solve
+// (cnns_init) and never change, so only 4 of the 16 bytes are written.
+__global__ void k_pack_spl(uint32_t n, const uint32_t* __restrict__ lab, float4* __restrict__ spl)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float4 v = sp[i];
-    v.w = __uint_as_float(lab[i]);
-    spl[i] = v;
+    reinterpret_cast<uint32_t*>(spl)[4 * (size_t)i + 3] = lab[i];
 }
 
 // Who searches in the first pass (flag 1), who waits for the second (2), who
@@ -462,7 +461,7 @@ cudaError_t cnns_node_labels(Ctx& c)
     if ((e = node_labels_of(c, c.lab.p, c.nlab.p)) != cudaSuccess) return e;
     if (!c.cnns_warp) {
         if ((e = ensure(c.spl, (size_t)c.n)) != cudaSuccess) return e;
-        k_pack_spl<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.sp.p, c.lab.p, c.spl.p);
+        k_pack_spl<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.spl.p);
         c.launches++;
     }
     return cudaGetLastError();
@@ -478,6 +477,10 @@ cudaError_t cnns_init(Ctx& c)
     if ((e = ensure(c.clb, n)) != cudaSuccess) return e;
     if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
     if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
+    // the packed points' coordinates, once per solve (each round writes the labels)
+    if ((e = cudaMemcpyAsync(c.spl.p, c.sp.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, c.stream)) !=
+        cudaSuccess)
+        return e;
     if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
     if (c.knn_seed && !c.cnns_warp) {
         if ((e = ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
