@@ -421,6 +421,13 @@ cudaError_t select_flagged_one(Ctx& c, uint32_t* out, uint32_t* count)
                                  FlagIsOne{c.dflag.p}, c.stream);
 }
 
+// input id -> leaf position (perm maps leaf position -> input id)
+__global__ void k_inverse_perm(uint32_t n, const uint32_t* __restrict__ perm, uint32_t* __restrict__ iperm)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) iperm[perm[j]] = j;
+}
+
 __global__ void k_fill_u32(uint32_t* __restrict__ p, uint32_t n, uint32_t v)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -485,6 +492,9 @@ cudaError_t cnns_init(Ctx& c)
     if (c.knn_seed && !c.cnns_warp) {
         if ((e = ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
         if ((e = ensure(c.kcur, n)) != cudaSuccess) return e;
+        if ((e = ensure(c.iperm, n)) != cudaSuccess) return e;
+        k_inverse_perm<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.perm.p, c.iperm.p);
+        c.launches++;
     }
     size_t tb = 0, tb2 = 0;
     if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
@@ -588,8 +598,8 @@ cudaError_t cnns_select(Ctx& c)
                 // host-driven rounds (profile mode) know the round: time the working launch
                 const bool timed = c.kernel_timer && c.round == 1;
                 if (timed) c.kernel_timer(c.timer_owner, 0, true);
-                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream)
-                                            : launch_knn_first3(a, pc != nullptr, c.klist.p, c.kcur.p, c.sms, c.stream);
+                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.klist.p, c.kcur.p, c.iperm.p, c.sms, c.stream)
+                                            : launch_knn_first3(a, pc != nullptr, c.klist.p, c.kcur.p, c.iperm.p, c.sms, c.stream);
                 if (ek != cudaSuccess) return ek;
                 if (timed) {
                     c.kernel_timer(c.timer_owner, 0, false);

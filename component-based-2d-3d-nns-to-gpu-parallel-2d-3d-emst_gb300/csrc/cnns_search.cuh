@@ -789,7 +789,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
 // the exact K nearest, as with one traversal per lane.
 template <int D, bool CL>
 __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ klist,
-                                                                unsigned char* __restrict__ kcur)
+                                                                unsigned char* __restrict__ kcur,
+                                                                const uint32_t* __restrict__ iperm)
 {
     if (*a.round != 1) return;
     const float4* __restrict__ spl = a.spl;
@@ -817,13 +818,11 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         const uint32_t labp = listed ? a.lab[me] : kEmpty;
         const float4 P = spl[me];
         const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
+        // the list: (d2 bits << 32 | input id), sorted; positions are looked
+        // up from the ids once at the end
         uint64_t kk[K];
-        uint32_t kp[K];
 #pragma unroll
-        for (int j = 0; j < K; ++j) {
-            kk[j] = kNoKey;
-            kp[j] = kNone;
-        }
+        for (int j = 0; j < K; ++j) kk[j] = kNoKey;
         // d2 of the K-th entry once the list is full, FLT_MAX before (every
         // finite bound and distance passes, an empty box's +inf does not);
         // lanes past the list's end take -1 so that no node and no candidate
@@ -878,13 +877,14 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 for (int j = 0; j < 32; ++j) {
                     const float4 c = pt[j];
                     const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                    // not a candidate: in the query's component (itself) or,
-                    // in a batch, in another cloud (lanes may hold different
-                    // clouds)
-                    bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
+                    // in a batch, a point of another cloud is no candidate
+                    // (lanes may hold different clouds)
+                    bool ok = d2 <= bd;
                     if constexpr (CL) ok = ok && s_cl[w][j] == qc;
                     mask |= (ok ? 1u : 0u) << j;
                 }
+                // round 1: the query's component is the query alone
+                if (leaf == (me >> 5)) mask &= ~(1u << (me & 31u));
             } else {
                 const float4 c = pt[lane];
                 const uint32_t cc = CL ? s_cl[w][lane] : 0u;
@@ -912,19 +912,14 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 if (d2 > bd) continue;
                 const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | ids[j];
                 if (key >= kk[K - 1]) continue;
-                const uint32_t pos = b + j;
                 // sorted insert, all in registers
 #pragma unroll
                 for (int t = K - 1; t > 0; --t) {
                     const bool sh = key < kk[t - 1];
                     const bool put = !sh && key < kk[t];
                     kk[t] = sh ? kk[t - 1] : (put ? key : kk[t]);
-                    kp[t] = sh ? kp[t - 1] : (put ? pos : kp[t]);
                 }
-                if (key < kk[0]) {
-                    kk[0] = key;
-                    kp[0] = pos;
-                }
+                if (key < kk[0]) kk[0] = key;
                 if (kk[K - 1] != kNoKey) bd = __uint_as_float((uint32_t)(kk[K - 1] >> 32));
             }
         };
@@ -962,10 +957,14 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 __syncwarp();
             }
         }
+        uint32_t p0 = kNone;  // entry 0's leaf position
         if (listed) {
 #pragma unroll
-            for (int j = 0; j < K; ++j)
-                klist[(size_t)j * n + me] = kk[j] == kNoKey ? ~0ull : ((kk[j] >> 32) << 32) | kp[j];
+            for (int j = 0; j < K; ++j) {
+                const uint32_t pos = kk[j] == kNoKey ? kNone : __ldg(&iperm[(uint32_t)kk[j]]);
+                if (j == 0) p0 = pos;
+                klist[(size_t)j * n + me] = kk[j] == kNoKey ? ~0ull : ((kk[j] >> 32) << 32) | pos;
+            }
             kcur[me] = 0;
         }
         // round-1 result: entry 0 (exact: every node within the K-th
@@ -978,7 +977,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 const uint32_t mn = (uint32_t)min(op, (int)(uint32_t)kk[0]);
                 const uint64_t key = ((uint64_t)__float_as_uint(d0) << 32) | mn;
                 a.lbp[me] = d0;
-                a.selq[me] = kp[0];
+                a.selq[me] = p0;
                 a.selkey[me] = key;
                 if (key <= __ldcg(&a.ckey[labp])) {
                     const uint64_t old = atomicMin((unsigned long long*)&a.ckey[labp], (unsigned long long)key);
@@ -1021,14 +1020,15 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 }
 
 template <int D, bool CL>
-cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, int sms, cudaStream_t s)
+cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, const uint32_t* iperm, int sms,
+                       cudaStream_t s)
 {
     constexpr int T = kKnnWarps * 32;
     uint64_t b = ((uint64_t)a.n + T - 1) / T;
     const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, klist, kcur);
+    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm);
     return cudaGetLastError();
 }
 

@@ -348,7 +348,7 @@ emst_status build_graph(emst_ctx* x)
                                     (const void*)(intptr_t)(c.learned ? 1 : 0), c.trace.p,
                                     (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p, c.snaps.p,
-                                    (const void*)(intptr_t)c.snap_cap, c.klist.p, c.kcur.p,
+                                    (const void*)(intptr_t)c.snap_cap, c.klist.p, c.kcur.p, c.iperm.p,
                                     (const void*)(intptr_t)(c.knn_seed ? 1 : 0)};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
@@ -510,6 +510,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.trace_ctl);
     emst::release(c.snaps);
     emst::release(c.klist);
+    emst::release(c.iperm);
     emst::release(c.kcur);
     emst::release(c.sel_tmp);
     emst::release(c.lbp);

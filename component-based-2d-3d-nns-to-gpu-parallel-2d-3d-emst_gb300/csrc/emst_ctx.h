@@ -166,6 +166,7 @@ struct Ctx {
     // d2 bits << 32 | leaf position, sorted by (d2, input id); ~0 = no entry
     DevBuf<uint64_t> klist;
     DevBuf<unsigned char> kcur;  // per point: leading list entries known to lie in its component
+    DevBuf<uint32_t> iperm;      // input id -> leaf position (the list build keeps ids, writes positions)
     // one search launch per round: the points the factor keeps first, the
     // others after them (instead of a second pass)
     bool first_pass_ordered = false;
@@ -297,10 +298,10 @@ cudaError_t proposal_trace_begin(Ctx& c);
 cudaError_t proposal_trace_end(Ctx& c);
 uint64_t splitmix(uint64_t& s);
 
-cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur, int sms,
-                             cudaStream_t s);
-cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur, int sms,
-                             cudaStream_t s);
+cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur,
+                             const uint32_t* iperm, int sms, cudaStream_t s);
+cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur,
+                             const uint32_t* iperm, int sms, cudaStream_t s);
 cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
 
