@@ -786,7 +786,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
 // every candidate instead of diverging over per-lane traversals.  Each leaf
 // reaches every lane at most once, and a lane's bound only shrinks, so every
 // lane still sees every point within its final K-th distance: the lists are
-// the exact K nearest, as with one traversal per lane.
+// the exact K nearest, as with one traversal per lane.  During the search a
+// list holds only its (d2 bits, input id) keys; each entry's leaf position is
+// read from iperm (input id -> position) once, when the list is written.
 template <int D, bool CL>
 __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ klist,
                                                                 unsigned char* __restrict__ kcur,
