@@ -154,8 +154,8 @@ __device__ __forceinline__ uint64_t spread3(uint32_t x)
     return v;
 }
 
-// Hilbert index of the cell x[0..D) on the order-21 (3D) / order-31 (2D)
-// curve, after J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
+// Hilbert index of the cell x[0..D) on the order-kBits curve (by default 21
+// in 3D, 31 in 2D: the widest that fit 64 bits), after J. Skilling, "Programming the Hilbert curve", AIP Conf. Proc.
 // 707, 381 (2004): the coordinates are turned in place into the transposed
 // index, whose bits, interleaved with axis 0 most significant in each group,
 // form the index.  Cells with consecutive indices share a face, so a run of
@@ -163,10 +163,10 @@ __device__ __forceinline__ uint64_t spread3(uint32_t x)
 // across the domain and leave a box that overlaps many others.  The curve
 // starts at the origin and fills each origin sub-cube before leaving it, so
 // cells below 2^b on every axis get indices below 2^(D*b).
-template <int D>
+template <int D, int kBits = (D == 3 ? 21 : 31)>
 __device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3])
 {
-    constexpr int kBits = D == 3 ? 21 : 31;
+    static_assert(kBits >= 1 && kBits * D <= 63, "the index must fit 63 bits");
     constexpr uint32_t top = 1u << (kBits - 1);
 #pragma unroll
     for (uint32_t q = top; q > 1; q >>= 1) {

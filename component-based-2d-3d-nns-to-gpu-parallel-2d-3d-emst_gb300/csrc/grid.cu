@@ -7,8 +7,9 @@
 //      InputRW.h:545-559) and the reference's unitX in double
 //      (SolutionEMST.cu:305-341);
 //   2. the rescale p' = float(float(p - pMin) * float(unitX)) (:361-364),
-//      fused with a 64-bit Hilbert cell key per point (21 bits/axis in 3D,
-//      31 bits/axis in 2D);
+//      fused with a 48-bit Hilbert cell key per point (16 bits/axis in 3D,
+//      24 bits/axis in 2D: cells 2^-16 / 2^-24 of the extent, finer than
+//      any leaf, and a 6-pass radix sort instead of 8);
 //   3. a radix sort of the cell keys, so points of one cell (and of
 //      neighbouring cells) are contiguous: leaves of 32 consecutive points
 //      have bounded occupancy whatever the density, unlike the reference's
@@ -27,6 +28,11 @@
 #include "emst_device.cuh"
 
 namespace emst {
+
+// bits per axis of the single-cloud cell key
+template <int D>
+constexpr int kCellBits = D == 3 ? 16 : 24;
+
 
 namespace {
 
@@ -140,7 +146,7 @@ __global__ void k_minmax_final(const float* __restrict__ part, int nblk, int64_t
     }
     np->unitx = ux;
     np->uxf = uxf;
-    const float qmax = D == 3 ? 2097151.f : 2147483520.f;  // 2^21-1; largest float below 2^31
+    const float qmax = (float)((1u << kCellBits<D>) - 1u);  // 2^16-1 / 2^24-1: exact in float
     np->qscale = smax > 0.f ? qmax / smax : 0.f;
 }
 
@@ -157,10 +163,10 @@ __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const Nor
     for (int c = 0; c < D; ++c) {
         float s = __fmul_rn(__fsub_rn(in[i * D + c], np->pmin[c]), uxf);
         scaled[i * D + c] = s;
-        float qf = fminf(fmaxf(__fmul_rn(s, qs), 0.f), D == 3 ? 2097151.f : 2147483520.f);
+        float qf = fminf(fmaxf(__fmul_rn(s, qs), 0.f), (float)((1u << kCellBits<D>) - 1u));
         cell[c] = (uint32_t)qf;
     }
-    key[i] = hilbert_index<D>(cell);
+    key[i] = hilbert_index<D, kCellBits<D>>(cell);
     idx[i] = (uint32_t)i;
 }
 
@@ -304,7 +310,7 @@ cudaError_t grid_build(Ctx& c)
         k_rescale_key<3><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p);
     }
     // Radix sort of the cell keys (only the significant bits).
-    const int end_bit = D == 3 ? 63 : 62;
+    const int end_bit = D * (D == 3 ? kCellBits<3> : kCellBits<2>);
     cub::DoubleBuffer<uint64_t> keys(c.mkey.p, c.mkey_alt.p);
     cub::DoubleBuffer<uint32_t> vals(c.perm.p, c.perm_alt.p);
     size_t tmp = 0;
