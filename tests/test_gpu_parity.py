@@ -470,7 +470,10 @@ def test_search_kernels_keep_edges(gpu_lib, kind, dim, n, mode):
     with gpu_lib.Emst(wide_search=-1) as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
-    for kw in (dict(), dict(host_rounds=True), dict(round1_neighbours=-1)):
+    # the first-pass rules send a second list (two passes) or a second list
+    # segment (one ordered launch) through the same kernels
+    for kw in (dict(), dict(host_rounds=True), dict(round1_neighbours=-1), dict(first_pass_factor=1.5),
+               dict(first_pass_factor=1.5, first_pass_ordered=True)):
         with gpu_lib.Emst(wide_search=mode, **kw) as e:
             uv, ln = e.solve(pts)
             assert np.array_equal(_canon(uv), _canon(ref)), kw
