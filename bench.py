@@ -511,8 +511,9 @@ def main():
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": args.workload, "n": n, "dim": dim, "rounds": rounds,
-                           "search": {0: "component: round-1 neighbour lists (warp per 32 queries), "
-                                         "later rounds thread per query", 1: "static region table",
+                           "search": {0: "component: round-1 neighbour lists (warp per 32 queries); later "
+                                         "rounds by query-list length: warp per query, thread per query, "
+                                         "warp per 32 queries", 1: "static region table",
                                       2: "component, warp per 32 queries"}[args.mode],
                            "l2": "512 MB buffer written between timed steps; working set > 129 MB L2",
                            "launch_shape": launch_shape,
