@@ -1,6 +1,15 @@
-// cnns_search.cuh -- the thread-per-query component search kernel, shared by
-// the per-dimension translation units that instantiate it for every launch
-// shape of the table (cnns_t2.cu, cnns_t3.cu).
+// cnns_search.cuh -- the component search kernels, shared by the
+// per-dimension translation units that instantiate them (cnns_t2.cu,
+// cnns_t3.cu): per searching point, its nearest point outside its component
+// under (d2, input id), folded into the component's key.  Together they take
+// the place of the reference's per-round search, the static region table
+// (K_computeOctants, NodeEMST.h:1018-1296) read by K_findNextClosestPoint
+// (NodeEMST.h:1303-1384), with the same per-component result (cnns.cu).
+//   k_knn_first  round 1: every point's kKnn nearest, warp per 32 queries
+//   k_cnns_w     later rounds, short query lists: warp per query
+//   k_cnns_t     later rounds, middle lists: thread per query (every launch
+//                shape of the table; the learned first pass runs here)
+//   k_cnns_c     later rounds, long lists: warp per 32 queries walking together
 #pragma once
 #include <cfloat>
 #include <climits>
