@@ -266,11 +266,14 @@ def learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, d
         q = max(p["search_queries"], 1)
         return {"searches_per_point": p["search_queries"] / n, "cells_visited_per_query": p["leaf_visits"] / q,
                 "cells_visited_per_point": p["leaf_visits"] / n, "node_tests_per_query": p["node_tests"] / q,
-                "first_pass_searches": p["first_pass_searches"], "deferred": p["first_pass_deferred"]}
+                "knn_candidates_marked_per_point": p["knn_marked"] / n,
+                "knn_insert_steps_per_warp": p["knn_insert_steps"] / max(n / 32, 1),
+                "knn_learned_queries": p["knn_learned"], "knn_resumed_queries": p["knn_resumed"],
+                "ms_knn": p["ms_knn"] / max(p["knn_launches"], 1)}
     return {"value": n * K / (sum(ms) / 1e3) / 1e6, "unit": "Mpoints/s", "ms_per_step": sum(ms) / K,
             "plain_value": n * len(plain_ms) / (sum(plain_ms) / 1e3) / 1e6, "vs_plain": sum(plain_ms) / len(plain_ms) / (sum(ms) / K),
             "same_edge_set": same, "margin": margin, "threshold": thr,
-            "mispredict_rate": pl["first_pass_resumed"] / max(pl["first_pass_searches"], 1),
+            "mispredict_rate": pl["knn_resumed"] / max(pl["knn_learned"], 1),
             "plain": per(pp), "learned": per(pl),
             "weights": {k: info.get(k) for k in ("records", "clouds", "points_per_cloud", "generator", "epochs",
                                                   "loss_curve")},

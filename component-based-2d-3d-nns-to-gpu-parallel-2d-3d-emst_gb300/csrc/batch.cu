@@ -20,10 +20,10 @@
 #include <climits>
 #include <cmath>
 
-#include <cub/device/device_radix_sort.cuh>
 
 #include "emst_ctx.h"
 #include "emst_device.cuh"
+#include "radix.cuh"
 
 namespace emst {
 
@@ -231,22 +231,22 @@ cudaError_t batch_grid_build(Ctx& c)
     const int nc = c.n_clouds;
     cudaStream_t s = c.stream;
     cudaError_t e;
-    if ((e = ensure(c.norm, (size_t)nc)) != cudaSuccess) return e;
-    if ((e = ensure(c.stage, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.mkey, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.mkey_alt, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.perm, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.perm_alt, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.sp, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.pcloud_in, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.pcloud, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.norm, (size_t)nc)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.stage, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.mkey, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.mkey_alt, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.perm, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.perm_alt, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.sp, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.pcloud_in, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.pcloud, (size_t)n)) != cudaSuccess) return e;
     c.nchunk = (n + kLeaf - 1) / kLeaf;
     c.L = 1;
     while (c.L < c.nchunk) c.L <<= 1;
-    if ((e = ensure(c.nlo, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.nhi, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.nid, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.ncloud, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nlo, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nhi, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nid, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.ncloud, (size_t)2 * c.L)) != cudaSuccess) return e;
 
     int cb = 1;
     while ((1 << cb) < nc) ++cb;
@@ -255,15 +255,20 @@ cudaError_t batch_grid_build(Ctx& c)
     k_batch_norm<<<nc, kThreads, 0, s>>>(c.in, c.d_off.p, c.d_foff.p, c.d_dims.p, c.norm.p, c.ctr.p, bits3, bits2);
     k_batch_rescale_key<<<nc, kThreads, 0, s>>>(c.in, c.d_off.p, c.d_foff.p, c.d_dims.p, c.norm.p, c.stage.p,
                                                 c.mkey.p, c.perm.p, c.pcloud_in.p, bits3, bits2, shift);
-    cub::DoubleBuffer<uint64_t> keys(c.mkey.p, c.mkey_alt.p);
-    cub::DoubleBuffer<uint32_t> vals(c.perm.p, c.perm_alt.p);
-    size_t tmp = 0;
-    if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys, vals, (int)n, 0, 63, s)) != cudaSuccess) return e;
-    if ((e = ensure(c.sort_tmp, tmp)) != cudaSuccess) return e;
-    if ((e = cub::DeviceRadixSort::SortPairs(c.sort_tmp.p, tmp, keys, vals, (int)n, 0, 63, s)) != cudaSuccess)
+    // (cloud << shift) | cell key: the cloud index takes the top bits of 63
+    const size_t tmp = radix_scratch_bytes(n, 63);
+    if ((e = c.ensure(c.sort_tmp, tmp)) != cudaSuccess) return e;
+    bool in_alt = false;
+    if ((e = radix_sort_pairs(c.mkey.p, c.mkey_alt.p, c.perm.p, c.perm_alt.p, n, 63, c.sort_tmp.p, tmp,
+                              &c.ctr.p->err, &in_alt, s)) != cudaSuccess)
         return e;
-    if (keys.Current() != c.mkey.p) std::swap(c.mkey.p, c.mkey_alt.p);
-    if (vals.Current() != c.perm.p) std::swap(c.perm.p, c.perm_alt.p);
+    c.launches += 2 + radix_passes(63);
+    if (in_alt) {
+        std::swap(c.mkey.p, c.mkey_alt.p);
+        std::swap(c.mkey.cap, c.mkey_alt.cap);
+        std::swap(c.perm.p, c.perm_alt.p);
+        std::swap(c.perm.cap, c.perm_alt.cap);
+    }
     k_batch_gather<<<blocks_for(n, 256), 256, 0, s>>>(c.stage.p, c.perm.p, c.pcloud_in.p, n, c.sp.p, c.pcloud.p);
     c.launches += 3;
     if ((e = leaf_tree(c)) != cudaSuccess) return e;
@@ -280,8 +285,8 @@ cudaError_t batch_output(Ctx& c, int32_t* d_uv, double* d_len)
     cudaError_t e;
     const int nc = c.n_clouds;
     const int64_t rows = c.n - c.n_nonempty;  // sum over clouds of (n_c - 1)
-    if ((e = ensure(c.bcursor, (size_t)nc)) != cudaSuccess) return e;
-    if ((e = ensure(c.bedges, (size_t)2 * (rows > 0 ? rows : 1))) != cudaSuccess) return e;
+    if ((e = c.ensure(c.bcursor, (size_t)nc)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.bedges, (size_t)2 * (rows > 0 ? rows : 1))) != cudaSuccess) return e;
     cudaMemsetAsync(c.bcursor.p, 0, sizeof(uint32_t) * nc, c.stream);
     if (c.n_edges)
         k_batch_edges<<<blocks_for(c.n_edges, 256), 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.pcloud_in.p,

@@ -348,19 +348,19 @@ cudaError_t boruvka_init(Ctx& c)
 {
     cudaError_t e;
     const size_t n = (size_t)c.n;
-    if ((e = ensure(c.lab, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.par, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.selq, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.selkey, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.ckey, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.cmax, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.act, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.act2, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.roots, 2 * n)) != cudaSuccess) return e;
-    if ((e = ensure(c.dcum, 128)) != cudaSuccess) return e;
-    if ((e = ensure(c.prov, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.edges, 2 * (n > 1 ? n - 1 : 1))) != cudaSuccess) return e;
-    if ((e = ensure(c.eround, n > 1 ? n - 1 : 1)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.lab, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.par, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.selq, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.selkey, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.ckey, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.cmax, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.act, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.act2, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.roots, 2 * n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.dcum, 128)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.prov, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.edges, 2 * (n > 1 ? n - 1 : 1))) != cudaSuccess) return e;
+    if ((e = c.ensure(c.eround, n > 1 ? n - 1 : 1)) != cudaSuccess) return e;
     k_init<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.par.p, c.roots.p, c.act.p,
                                                         c.ckey.p, c.cmax.p);
     c.n_act = (uint32_t)c.n;
@@ -374,7 +374,14 @@ cudaError_t boruvka_flatten(Ctx& c)
     DevCounters* d = c.ctr.p;
     const uint32_t n = (uint32_t)c.n;
     k_jump<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, n, c.par.p, &d->err);
-    k_relabel<<<blocks_for((c.n + 3) / 4, 256), 256, 0, c.stream>>>(n, c.lab.p, c.par.p);
+    if (c.search_mode == 0) {
+        // component search: the relabel also writes the next round's node labels
+        cudaError_t e = node_labels_of(c, c.lab.p, c.nlab.p, c.par.p);
+        if (e != cudaSuccess) return e;
+        c.launches--;  // counted below with the relabel
+    } else {
+        k_relabel<<<blocks_for((c.n + 3) / 4, 256), 256, 0, c.stream>>>(n, c.lab.p, c.par.p);
+    }
     k_flatten_begin<<<1, 1, 0, c.stream>>>(d);
     k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, n, c.par.p, c.ckey.p, c.cmax.p,
                                                                 c.search_mode == 0 ? c.clb.p : nullptr);
@@ -449,7 +456,7 @@ cudaError_t evaluate_length(Ctx& c, double* d_out)
 {
     cudaError_t e;
     const unsigned nb = list_grid(c.n_edges ? c.n_edges : 1);
-    if ((e = ensure(c.lpart, nb)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.lpart, nb)) != cudaSuccess) return e;
     if (c.dim == 2)
         k_edge_len<2><<<nb, 256, 0, c.stream>>>(c.edges.p, c.n_edges, c.in, c.lpart.p);
     else

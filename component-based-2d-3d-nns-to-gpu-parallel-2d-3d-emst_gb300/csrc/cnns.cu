@@ -28,8 +28,6 @@
 #include <climits>
 #include <cmath>
 
-#include <cub/device/device_select.cuh>
-#include <thrust/iterator/counting_iterator.h>
 
 #include "cnns_search.cuh"
 
@@ -48,10 +46,13 @@ __device__ __forceinline__ uint32_t merge_label(uint32_t a, uint32_t b)
 }
 
 // Leaves of one block (a subtree of kLeavesPerBlock leaf slots, or all of L
-// when smaller) and the levels above them inside that subtree.
+// when smaller) and the levels above them inside that subtree.  With `par`
+// (the flatten step) every point's label is first replaced by its root's
+// root, lab[j] = par[lab[j]] (K_EMST_flatten_DST_1, EMSTOperators.h:412-433),
+// so the relabel and the next round's node labels take one pass over lab.
 __global__ void __launch_bounds__(1024)
-    k_node_labels_sub(const uint32_t* __restrict__ lab, uint32_t n, uint32_t nchunk, uint32_t L, uint32_t span,
-                      uint32_t* __restrict__ nlab)
+    k_node_labels_sub(uint32_t* __restrict__ lab, const uint32_t* __restrict__ par, uint32_t n, uint32_t nchunk,
+                      uint32_t L, uint32_t span, uint32_t* __restrict__ nlab)
 {
     __shared__ uint32_t s[kLeavesPerBlock];
     const uint32_t first = blockIdx.x * span;
@@ -62,7 +63,11 @@ __global__ void __launch_bounds__(1024)
         if (c < nchunk) {
             const uint32_t j = c * 32 + lane;
             const bool v = j < n;
-            const uint32_t my = v ? lab[j] : 0u;
+            uint32_t my = v ? lab[j] : 0u;
+            if (par && v) {
+                my = __ldcg(&par[my]);
+                lab[j] = my;
+            }
             const uint32_t l0 = __shfl_sync(kFull, my, 0);
             out = __all_sync(kFull, !v || my == l0) ? l0 : kMixed;
         }
@@ -343,82 +348,210 @@ __global__ void __launch_bounds__(WPB * 32)
     }
 }
 
-// Per round: each point's current component label into the .w word of its
-// packed (x, y, z, label) record.  The coordinates are copied once per solve
-// (cnns_init) and never change, so only 4 of the 16 bytes are written.
-__global__ void k_pack_spl(uint32_t n, const uint32_t* __restrict__ lab, float4* __restrict__ spl)
+// Query lists of a search pass, compacted in leaf order (a warp's 32
+// queries are neighbours, so their traversals share nodes and cache lines;
+// in round 1 every warp's queries are exactly one leaf).  Three launches:
+// k_sel_count decides each point's list and counts per tile of kSelTile
+// consecutive points, k_sel_scan turns the tile counts into offsets (one
+// block), k_sel_write writes every tile's points at its offset in order.
+//   stage 0 (first pass): a dirty point (flag != 0) whose lower bound exceeds
+//     its component's key (set by the reused partners) cannot hold the
+//     component's minimum and leaves the round (flag 0); one whose bound
+//     exceeds `factor` times its component's smallest waits for the second
+//     pass (flag 2, written to list2 when one is given); the others search
+//     now (flag 1, list1).
+//   stage 1 (second pass): a waiting point (flag 2) whose bound the first
+//     pass did not rule out searches (list1); every flag ends at 0.
+//   stage 2: every flagged point, unfiltered (list1); flags unchanged.
+constexpr int kSelThreads = 256, kSelItems = 8, kSelTile = kSelThreads * kSelItems;
+constexpr int kScanThreads = 1024;
+constexpr unsigned char kSelPicked = 3;  // stage 1: selected, cleared by k_sel_write
+
+__device__ __forceinline__ void load_flags(const unsigned char* __restrict__ flag, uint32_t p0, uint32_t n,
+                                           unsigned char (&f)[kSelItems])
 {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    reinterpret_cast<uint32_t*>(spl)[4 * (size_t)i + 3] = lab[i];
+    if (p0 + kSelItems <= n) {
+        const uint2 v = *reinterpret_cast<const uint2*>(flag + p0);  // p0 is a multiple of 8
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            f[k] = (unsigned char)(v.x >> (8 * k));
+            f[4 + k] = (unsigned char)(v.y >> (8 * k));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k) f[k] = p0 + k < n ? flag[p0 + k] : 0;
+    }
 }
 
-// Who searches in the first pass (flag 1), who waits for the second (2), who
-// needs no search this round (0), decided before the search so that search
-// warps carry only real searches.  A dirty point whose lower bound exceeds
-// its component's key (set by reused partners) cannot hold the minimum; one
-// whose bound exceeds `factor` times its component's smallest waits.
-__global__ void k_filter_first(uint32_t n, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
-                               const float* __restrict__ lbp, const uint64_t* __restrict__ ckey,
-                               const uint32_t* __restrict__ clb, float factor, unsigned long long* __restrict__ stats)
+// Which list a point's (new) flag puts it on: 0 none, 1 list1, 2 list2.
+__device__ __forceinline__ int list_of(int stage, unsigned char f, bool two)
 {
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-        const uint32_t p = base + threadIdx.x;
-        bool later = false;
-        if (p < n && flag[p]) {
+    if (stage == 0) return f == 1 ? 1 : (f == 2 && two ? 2 : 0);
+    if (stage == 1) return f == kSelPicked ? 1 : 0;
+    return f ? 1 : 0;
+}
+
+// Block-wide exclusive scan of a packed (list1 count | list2 count << 16).
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* s_warp, uint32_t& total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_warp[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const uint32_t x = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0u;
+        uint32_t in = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(kFull, in, o);
+            if (lane >= o) in += t;
+        }
+        if (lane < (int)(blockDim.x >> 5)) s_warp[lane] = in - x;
+        if (lane == (int)(blockDim.x >> 5) - 1) s_warp[32] = in;
+    }
+    __syncthreads();
+    const uint32_t ex = s_warp[w] + incl - v;
+    total = s_warp[32];
+    __syncthreads();  // s_warp is reused by the caller's next scan
+    return ex;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+    k_sel_count(uint32_t n, int stage, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
+                const float* __restrict__ lbp, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ clb,
+                float factor, bool two, uint32_t* __restrict__ tile_cnt, unsigned long long* __restrict__ stats)
+{
+    __shared__ uint32_t s_warp[33];
+    const uint32_t tile = blockIdx.x;
+    const uint32_t p0 = tile * kSelTile + threadIdx.x * kSelItems;
+    unsigned char f[kSelItems];
+    load_flags(flag, p0, n, f);
+    uint32_t mine = 0, later = 0;
+    bool changed = false;
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k) {
+        const uint32_t p = p0 + k;
+        unsigned char nf = f[k];
+        if (f[k] && stage != 2) {
             const uint32_t l = lab[p];
             const float lb = lbp[p];
-            const uint64_t k = __ldcg(&ckey[l]);
-            const float cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
-            later = !(lb > cb) && lb > factor * __uint_as_float(__ldcg(&clb[l]));
-            flag[p] = lb > cb ? 0 : (later ? 2 : 1);
+            const uint64_t key = __ldcg(&ckey[l]);
+            const float cb = key == kNoKey ? INFINITY : __uint_as_float((uint32_t)(key >> 32));
+            if (stage == 0) {
+                nf = 0;
+                if (!(lb > cb)) nf = lb > factor * __uint_as_float(__ldcg(&clb[l])) ? 2 : 1;
+                later += nf == 2;
+            } else {
+                nf = (f[k] == 2 && !(lb > cb)) ? kSelPicked : 0;
+            }
         }
-        if (stats) {
-            const unsigned m = __ballot_sync(kFull, later);
-            if ((threadIdx.x & 31) == 0 && m) atomicAdd(&stats[7], (unsigned long long)__popc(m));
-        }
+        changed |= nf != f[k];
+        f[k] = nf;
+        const int o = list_of(stage, nf, two);
+        mine += o == 1 ? 1u : (o == 2 ? 0x10000u : 0u);
+    }
+    if (changed) {
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k)
+            if (p0 + k < n) flag[p0 + k] = f[k];
+    }
+    uint32_t total = 0;
+    block_exclusive(mine, s_warp, total);
+    if (threadIdx.x == 0) tile_cnt[tile] = total;
+    if (stats && stage == 0) {
+        for (int o = 16; o > 0; o >>= 1) later += __shfl_xor_sync(kFull, later, o);
+        if ((threadIdx.x & 31) == 0 && later) atomicAdd(&stats[7], (unsigned long long)later);
     }
 }
 
-// Second-pass searchers: waiting points (2) whose bound the first pass did
-// not rule out.
-__global__ void k_filter_second(uint32_t n, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
-                                const float* __restrict__ lbp, const uint64_t* __restrict__ ckey)
+// Exclusive offsets of the tiles' packed counts, in place; the totals go to
+// the list counters.  One block; each thread scans a run of tiles.
+__global__ void __launch_bounds__(kScanThreads)
+    k_sel_scan(uint32_t tiles, uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ cnt1, uint32_t* __restrict__ cnt2)
 {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const unsigned char f = flag[p];
-    if (!f) return;
-    bool go = false;
-    if (f == 2) {
-        const uint64_t k = __ldcg(&ckey[lab[p]]);
-        go = k == kNoKey || !(lbp[p] > __uint_as_float((uint32_t)(k >> 32)));
+    __shared__ uint32_t s_warp[33];
+    const uint32_t per = (tiles + kScanThreads - 1) / kScanThreads;
+    const uint32_t t0 = threadIdx.x * per;
+    // packed sums: a run holds at most per * kSelTile points per list, and the
+    // whole list at most n < 2^31; the two halves are kept apart in 64 bits
+    uint64_t run1 = 0, run2 = 0;
+    for (uint32_t t = t0; t < t0 + per && t < tiles; ++t) {
+        run1 += tile_cnt[t] & 0xffffu;
+        run2 += tile_cnt[t] >> 16;
     }
-    flag[p] = go ? 1 : 0;
+    // two block scans (32-bit each: list lengths are below 2^31)
+    uint32_t tot1 = 0, tot2 = 0;
+    uint32_t ex1 = block_exclusive((uint32_t)run1, s_warp, tot1);
+    uint32_t ex2 = block_exclusive((uint32_t)run2, s_warp, tot2);
+    for (uint32_t t = t0; t < t0 + per && t < tiles; ++t) {
+        const uint32_t v = tile_cnt[t];
+        // offsets do not fit 16 bits: list1 offsets in tile_cnt, list2 offsets
+        // in the second half of the array
+        tile_cnt[t] = ex1;
+        tile_cnt[tiles + t] = ex2;
+        ex1 += v & 0xffffu;
+        ex2 += v >> 16;
+    }
+    if (threadIdx.x == 0) {
+        *cnt1 = tot1;
+        if (cnt2) *cnt2 = tot2;
+    }
 }
 
-struct FlagIsOne {
-    const unsigned char* f;
-    __host__ __device__ bool operator()(uint32_t i) const { return f[i] == 1; }
-};
-
-struct FlagIsTwo {
-    const unsigned char* f;
-    __host__ __device__ bool operator()(uint32_t i) const { return f[i] == 2; }
-};
-
-cudaError_t select_flagged_two(Ctx& c, uint32_t* out, uint32_t* count)
+__global__ void __launch_bounds__(kSelThreads)
+    k_sel_write(uint32_t n, int stage, unsigned char* __restrict__ flag, bool two, const uint32_t* __restrict__ tile_off,
+                uint32_t tiles, uint32_t* __restrict__ list1, uint32_t* __restrict__ list2)
 {
-    size_t tb = c.sel_tmp.cap;
-    return cub::DeviceSelect::If(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), out, count, (int)c.n,
-                                 FlagIsTwo{c.dflag.p}, c.stream);
+    __shared__ uint32_t s_warp[33];
+    const uint32_t tile = blockIdx.x;
+    const uint32_t p0 = tile * kSelTile + threadIdx.x * kSelItems;
+    unsigned char f[kSelItems];
+    load_flags(flag, p0, n, f);
+    uint32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k) {
+        const int o = list_of(stage, f[k], two);
+        mine += o == 1 ? 1u : (o == 2 ? 0x10000u : 0u);
+    }
+    uint32_t total = 0;
+    const uint32_t ex = block_exclusive(mine, s_warp, total);
+    if (total == 0) return;
+    uint32_t o1 = tile_off[tile] + (ex & 0xffffu);
+    uint32_t o2 = two ? tile_off[tiles + tile] + (ex >> 16) : 0u;
+    bool clear = false;
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k) {
+        const uint32_t p = p0 + k;
+        const int o = list_of(stage, f[k], two);
+        if (o == 1) list1[o1++] = p;
+        else if (o == 2) list2[o2++] = p;
+        clear |= stage == 1 && f[k] == kSelPicked;
+    }
+    if (clear) {
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k)
+            if (p0 + k < n && f[k] == kSelPicked) flag[p0 + k] = 0;
+    }
 }
 
-cudaError_t select_flagged_one(Ctx& c, uint32_t* out, uint32_t* count)
+// A search pass's list (see k_sel_count).  Three launches.
+cudaError_t select_list(Ctx& c, int stage, float factor, uint32_t* list1, uint32_t* cnt1, uint32_t* list2,
+                        uint32_t* cnt2, unsigned long long* stats)
 {
-    size_t tb = c.sel_tmp.cap;
-    return cub::DeviceSelect::If(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), out, count, (int)c.n,
-                                 FlagIsOne{c.dflag.p}, c.stream);
+    const uint32_t tiles = (uint32_t)((c.n + kSelTile - 1) / kSelTile);
+    const bool two = list2 != nullptr;
+    k_sel_count<<<tiles, kSelThreads, 0, c.stream>>>((uint32_t)c.n, stage, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
+                                                     c.clb.p, factor, two, c.sel_tiles.p, stats);
+    k_sel_scan<<<1, kScanThreads, 0, c.stream>>>(tiles, c.sel_tiles.p, cnt1, two ? cnt2 : nullptr);
+    k_sel_write<<<tiles, kSelThreads, 0, c.stream>>>((uint32_t)c.n, stage, c.dflag.p, two, c.sel_tiles.p, tiles,
+                                                     list1, list2);
+    c.launches += 3;
+    return cudaGetLastError();
 }
 
 // input id -> leaf position (perm maps leaf position -> input id)
@@ -446,11 +579,12 @@ unsigned list_grid(uint64_t upper)
 
 // Tree-node labels: the value (component, or cloud) shared by all points of
 // a subtree, MIXED when they differ.
-cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out)
+cudaError_t node_labels_of(Ctx& c, uint32_t* labels, uint32_t* out, const uint32_t* par)
 {
     const uint32_t L = (uint32_t)c.L;
     const uint32_t span = L < (uint32_t)kLeavesPerBlock ? L : (uint32_t)kLeavesPerBlock;
-    k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(labels, (uint32_t)c.n, (uint32_t)c.nchunk, L, span, out);
+    k_node_labels_sub<<<L / span, 1024, 0, c.stream>>>(labels, par, (uint32_t)c.n, (uint32_t)c.nchunk, L, span,
+                                                       out);
     c.launches++;
     if (L / span >= 2) {
         k_node_labels_top<<<1, 1024, 0, c.stream>>>(L / span, out);
@@ -459,18 +593,13 @@ cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out)
     return cudaGetLastError();
 }
 
-// Per-round node labels (the component shared by all points of a subtree)
-// and the packed (x, y, z, label) points of the thread-per-query search.
+// Node labels of the initial forest (every point its own component); the
+// flatten step of every round refreshes them (boruvka.cu).
 cudaError_t cnns_node_labels(Ctx& c)
 {
     cudaError_t e;
-    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;  // no-op after cnns_init
+    if ((e = c.ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;  // no-op after cnns_init
     if ((e = node_labels_of(c, c.lab.p, c.nlab.p)) != cudaSuccess) return e;
-    if (!c.cnns_warp) {
-        if ((e = ensure(c.spl, (size_t)c.n)) != cudaSuccess) return e;
-        k_pack_spl<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.spl.p);
-        c.launches++;
-    }
     return cudaGetLastError();
 }
 
@@ -478,37 +607,27 @@ cudaError_t cnns_init(Ctx& c)
 {
     cudaError_t e;
     const size_t n = (size_t)c.n;
-    if ((e = ensure(c.dirty, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.dirty2, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.lbp, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.clb, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.spl, n)) != cudaSuccess) return e;
-    // the packed points' coordinates, once per solve (each round writes the labels)
-    if ((e = cudaMemcpyAsync(c.spl.p, c.sp.p, n * sizeof(float4), cudaMemcpyDeviceToDevice, c.stream)) !=
-        cudaSuccess)
-        return e;
-    if ((e = ensure(c.dflag, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.dirty, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.dirty2, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.lbp, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.clb, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nlab, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.dflag, n)) != cudaSuccess) return e;
+    // per tile of the list compaction: counts, then list1 and list2 offsets
+    if ((e = c.ensure(c.sel_tiles, 2 * ((n + kSelTile - 1) / kSelTile))) != cudaSuccess) return e;
     if (c.knn_seed && !c.cnns_warp) {
-        if ((e = ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
-        if ((e = ensure(c.kcur, n)) != cudaSuccess) return e;
-        if ((e = ensure(c.iperm, n)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.kcur, n)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.iperm, n)) != cudaSuccess) return e;
         k_inverse_perm<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.perm.p, c.iperm.p);
         c.launches++;
     }
-    size_t tb = 0, tb2 = 0;
-    if ((e = cub::DeviceSelect::Flagged(nullptr, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
-                                        &c.ctr.p->n_dirty, (int)n, c.stream)) != cudaSuccess)
-        return e;
-    if ((e = cub::DeviceSelect::If(nullptr, tb2, thrust::counting_iterator<uint32_t>(0), c.dirty.p,
-                                   &c.ctr.p->n_dirty, (int)n, FlagIsOne{c.dflag.p}, c.stream)) != cudaSuccess)
-        return e;
-    if ((e = ensure(c.sel_tmp, std::max(tb, tb2))) != cudaSuccess) return e;
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
     cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
     c.launches += 2;
-    return cudaGetLastError();
+    // node labels of the initial forest; each round's flatten refreshes them
+    return cnns_node_labels(c);
 }
 
 // Reuse pass + two search passes over the dirty points; fills ckey and the
@@ -523,25 +642,14 @@ cudaError_t cnns_select(Ctx& c)
     c.launches++;
     // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
-    cudaError_t e;
     unsigned long long* st = c.profile ? c.nstats.p : nullptr;
+    cudaError_t e;
     if (c.cnns_warp) {
-        size_t tb = c.sel_tmp.cap;
-        e = cub::DeviceSelect::Flagged(c.sel_tmp.p, tb, thrust::counting_iterator<uint32_t>(0), c.dflag.p, c.dirty.p,
-                                       &d->n_dirty, (int)c.n, c.stream);
-        c.launches += 2;  // a CUB selection is two kernels
+        e = select_list(c, 2, INFINITY, c.dirty.p, &d->n_dirty, nullptr, nullptr, st);
     } else {
-        // the learned proposal makes the first-pass choice itself
-        const float first_factor = c.learned && !c.n_clouds ? INFINITY : c.first_pass_factor;
-        k_filter_first<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
-                                                              c.clb.p, first_factor, st);
-        c.launches++;
-        e = select_flagged_one(c, c.dirty.p, &d->n_dirty);
-        c.launches += 2;
-        if (e == cudaSuccess && c.first_pass_ordered && !(c.learned && !c.n_clouds)) {
-            e = select_flagged_two(c, c.dirty2.p, &d->n_dirty2);
-            c.launches += 2;
-        }
+        const bool ordered = c.first_pass_ordered;
+        e = select_list(c, 0, c.first_pass_factor, c.dirty.p, &d->n_dirty, ordered ? c.dirty2.p : nullptr,
+                        ordered ? &d->n_dirty2 : nullptr, st);
     }
     if (e != cudaSuccess) return e;
     constexpr int WPB = 4;
@@ -549,9 +657,9 @@ cudaError_t cnns_select(Ctx& c)
     const uint32_t* pc = c.n_clouds ? c.pcloud.p : nullptr;
     const uint32_t* nc = c.n_clouds ? c.ncloud.p : nullptr;
     // A second pass has work only if something can defer a point: a finite
-    // first-pass factor, the learned proposal (single clouds), or the warp
-    // search's defer list.  Otherwise it is left out of the round.
-    const bool two_passes = c.cnns_warp || (c.learned && !pc) || !std::isinf(c.first_pass_factor);
+    // first-pass factor or the warp search's defer list.  Otherwise it is
+    // left out of the round.
+    const bool two_passes = c.cnns_warp || !std::isinf(c.first_pass_factor);
     for (int pass = 1; pass <= (two_passes ? 2 : 1); ++pass) {
         const uint32_t* list = pass == 1 ? c.dirty.p : c.dirty2.p;
         const uint32_t* cnt = pass == 1 ? &d->n_dirty : &d->n_dirty2;
@@ -567,13 +675,10 @@ cudaError_t cnns_select(Ctx& c)
                     c.selq.p, c.selkey.p, c.prov.p, &d->n_prov, c.lbp.p, c.clb.p, pass, c.dirty2.p, &d->n_dirty2,
                     st);
         } else {
-            CnnsArgs a{c.spl.p,  c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
+            CnnsArgs a{c.sp.p,   c.perm.p, c.nlo.p,   c.nhi.p, c.nlab.p, (uint32_t)c.n, (uint32_t)c.L, list,
                        cnt,      c.lab.p,  c.ckey.p,  c.selq.p, c.selkey.p, c.prov.p, &d->n_prov,  c.lbp.p,
                        c.clb.p,  pass,     c.dflag.p, pc,      nc,        st,       c.pfrag.p, c.margin,
                        c.threshold, &d->round,   nullptr,  nullptr,   knn};
-            // the learned first pass steers the lists k_cnns_t takes (its
-            // inference runs there); the other kernels search theirs plainly
-            // and defer nothing
             a.wide_limit = 0u;
             a.coop_min = kNoCoop;
             switch (c.search_split) {
@@ -582,24 +687,31 @@ cudaError_t cnns_select(Ctx& c)
             case 2: a.coop_min = 0u; break;
             default: break;
             }
-            const bool ordered = c.first_pass_ordered && !(c.learned && !pc);
+            const bool ordered = c.first_pass_ordered;
             if (ordered) {  // both segments in this one launch; no second pass
                 if (pass == 2) continue;
                 a.list2 = c.dirty2.p;
                 a.n_list2 = &d->n_dirty2;
             }
             const int shape = search_shape_of(c);
-            const bool learned = c.learned && pass == 1 && !pc;
-            if (pass == 1 && c.trace_cap > 0 && !learned) {
-                cudaError_t et = proposal_trace_begin(c);
-                if (et != cudaSuccess) return et;
-            }
             if (knn && pass == 1) {  // round 1 only (decided on the device)
+                // the learned proposal steers the list build's starting bound
+                // (single clouds); traces record the plain build
+                const bool learned = c.learned && !pc;
+                if (c.trace_cap > 0 && !learned && !pc) {
+                    a.trace = c.trace.p;
+                    a.trace_ctl = c.trace_ctl.p;
+                    a.trace_cap = (uint64_t)c.trace_cap;
+                    a.trace_mask = (1u << c.trace_shift) - 1u;
+                }
                 // host-driven rounds (profile mode) know the round: time the working launch
                 const bool timed = c.kernel_timer && c.round == 1;
                 if (timed) c.kernel_timer(c.timer_owner, 0, true);
-                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, c.klist.p, c.kcur.p, c.iperm.p, c.sms, c.stream)
-                                            : launch_knn_first3(a, pc != nullptr, c.klist.p, c.kcur.p, c.iperm.p, c.sms, c.stream);
+                cudaError_t ek = c.dim == 2 ? launch_knn_first2(a, pc != nullptr, learned, c.klist.p, c.kcur.p,
+                                                                c.iperm.p, c.sms, c.stream)
+                                            : launch_knn_first3(a, pc != nullptr, learned, c.klist.p, c.kcur.p,
+                                                                c.iperm.p, c.sms, c.stream);
+                a.trace = nullptr;
                 if (ek != cudaSuccess) return ek;
                 if (timed) {
                     c.kernel_timer(c.timer_owner, 0, false);
@@ -610,8 +722,8 @@ cudaError_t cnns_select(Ctx& c)
             // the component search has no work in round 1 when the lists ran
             const bool timed = c.kernel_timer && !(knn && c.round == 1);
             if (timed) c.kernel_timer(c.timer_owner, 1, true);
-            cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, learned, shape, c.sms, c.stream)
-                                        : launch_cnns_t3(a, pc != nullptr, learned, shape, c.sms, c.stream);
+            cudaError_t e1 = c.dim == 2 ? launch_cnns_t2(a, pc != nullptr, shape, c.sms, c.stream)
+                                        : launch_cnns_t3(a, pc != nullptr, shape, c.sms, c.stream);
             if (e1 != cudaSuccess) return e1;
             if (a.wide_limit > 0) c.launches++;         // k_cnns_w beside k_cnns_t
             if (a.coop_min != kNoCoop) c.launches++;  // k_cnns_c beside them
@@ -620,20 +732,12 @@ cudaError_t cnns_select(Ctx& c)
                 c.search_timed++;
             }
             if (pass == 1 && !ordered && two_passes) {
-                k_filter_second<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.dflag.p, c.lab.p,
-                                                                             c.lbp.p, c.ckey.p);
-                c.launches++;
-                cudaError_t e2 = select_flagged_one(c, c.dirty2.p, &d->n_dirty2);
+                cudaError_t e2 = select_list(c, 1, INFINITY, c.dirty2.p, &d->n_dirty2, nullptr, nullptr, nullptr);
                 if (e2 != cudaSuccess) return e2;
-                c.launches += 2;
             }
         }
         c.nns_launches++;
         c.launches++;
-    }
-    if (c.trace_cap > 0 && !(c.learned && !pc)) {
-        cudaError_t et = proposal_trace_end(c);
-        if (et != cudaSuccess) return et;
     }
     return cudaGetLastError();
 }

@@ -6,9 +6,10 @@
 // (K_computeOctants, NodeEMST.h:1018-1296) read by K_findNextClosestPoint
 // (NodeEMST.h:1303-1384), with the same per-component result (cnns.cu).
 //   k_knn_first  round 1: every point's kKnn nearest, warp per 32 queries
+//                (the learned proposal steers its starting bound)
 //   k_cnns_w     later rounds, short query lists: warp per query
 //   k_cnns_t     later rounds, middle lists: thread per query (every launch
-//                shape of the table; the learned first pass runs here)
+//                shape of the table)
 //   k_cnns_c     later rounds, long lists: warp per 32 queries walking together
 #pragma once
 #include <cfloat>
@@ -41,6 +42,16 @@ __device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* l
     if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = val;
 }
 
+// Training-trace sampling: a fixed hash of the point's leaf position.
+__device__ __forceinline__ uint32_t knn_sample_hash(uint32_t me)
+{
+    uint32_t h = me * 0x9E3779B1u ^ 0x27d4eb2fu;
+    h ^= h >> 15;
+    h *= 0x2c1b3c6du;
+    h ^= h >> 12;
+    return h;
+}
+
 // One thread per dirty point, each with its own traversal order: its own
 // leaf first, then a depth-first walk from the root pushing the nearer child
 // last, so every query sees good bounds early (queries of later rounds are
@@ -48,13 +59,11 @@ __device__ __forceinline__ void warp_append(bool pred, uint32_t val, uint32_t* l
 // CL: batched clouds (pcloud / ncloud given); a candidate must share the
 // query's cloud.
 // TPB threads per block, at least MINB blocks resident per SM (the launch
-// shape; kSearchShapes lists the instantiated pairs).  LEARN: first pass
-// under the learned proposal (proposal.cuh) instead of the fixed rule.
-template <int D, bool CL, int TPB, int MINB, bool LEARN = false>
+// shape; kSearchShapes lists the instantiated pairs).
+template <int D, bool CL, int TPB, int MINB>
 __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
 {
-    const float4* __restrict__ spl = a.spl;
-    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ sp = a.sp;
     const float4* __restrict__ nlo = a.nlo;
     const float4* __restrict__ nhi = a.nhi;
     const uint32_t* __restrict__ nlab = a.nlab;
@@ -68,7 +77,6 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     uint32_t* __restrict__ prov = a.prov;
     uint32_t* __restrict__ n_prov = a.n_prov;
     float* __restrict__ lbp = a.lbp;
-    const uint32_t* __restrict__ clb = a.clb;
     const int pass = a.pass;
     unsigned char* __restrict__ dflag = a.dflag;
     const uint32_t* __restrict__ pcloud = a.pcloud;
@@ -76,10 +84,6 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
     unsigned long long* __restrict__ stats = a.stats;
     constexpr int kTStack = 48;
     if (a.knn_round1 && *a.round == 1) return;  // round 1 is k_knn_first's
-    // learned proposal: weights stay in global memory (read-only cache); the
-    // kernel uses no shared memory, so the SM keeps its whole L1 for the search
-    const prop::Frag* W = reinterpret_cast<const prop::Frag*>(a.frag);
-    const int round = LEARN ? *a.round : 0;
     // the queries: list, then (one launch, second segment) list2
     const uint32_t n1 = *n_list;
     const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
@@ -91,60 +95,32 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
         const uint32_t me = listed ? (qi < n1 ? list[qi] : a.list2[qi - n1]) : 0u;
         const uint32_t labp = listed ? lab[me] : kEmpty;
         const float lb0 = listed ? lbp[me] : 0.f;
-        bool valid = listed, deferred = false;
+        bool valid = listed;
         float cb = INFINITY;
-        float cap = INFINITY;  // first-pass search radius (learned proposal)
         if (listed) {
             const uint64_t k = __ldcg(&ckey[labp]);
             cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
             if (lb0 > cb) valid = false;  // cannot hold its component's minimum this round
         }
-        if constexpr (LEARN) {
-            // the whole warp is converged here: one tensor-core inference for
-            // its 32 queries, features in registers
-            float f[prop::kIn];
-            if (listed) {
-                const uint32_t ol = L + (me >> 5);
-                const float4 lo = __ldg(&nlo[ol]), hi = __ldg(&nhi[ol]);
-                const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = D == 3 ? hi.z - lo.z : 0.f;
-                prop::features(lb0, __uint_as_float(__ldcg(&clb[labp])), cb, ex * ex + ey * ey + ez * ez,
-                               __ldg(&nlab[ol]) == labp, round, f);
-            } else {
-#pragma unroll
-                for (int i = 0; i < prop::kIn; ++i) f[i] = 0.f;
-            }
-            float o0, o1;
-            prop::infer_warp(W, f, o0, o1);
-            if (valid) {
-                cap = exp2f(fminf(8.f * o0 + a.margin, 126.f));
-                if (o1 < a.threshold || cap < lb0) {
-                    valid = false;  // predicted not to hold the minimum: second pass
-                    deferred = true;
-                }
-            }
-        }
-        bool again = false;  // first-pass search cut short by the proposal's radius
 
         bool record = false;
         uint32_t st_leaves = 0, st_nodes = 0, st_cands = 0;
         if (valid) {
-            const float4 P = spl[me];
-            const int op = (int)perm[me];
+            const float4 P = sp[me];
+            const int op = __float_as_int(P.w);
             const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;  // the query's cloud (batches)
             float bd = INFINITY, cut = INFINITY;
-            bool capped = false;  // a node was left out only by the radius
-            int bo = -1;  // input id of the best, loaded lazily (-1: not loaded)
-            int bs = -1;  // leaf position of the best
+            int bo = INT_MAX;  // input id of the best
+            int bs = -1;       // leaf position of the best
 
-            // spl holds (x, y, z, label bits); input ids are needed only to
-            // break exact d2 ties and for the final key.
+            // sp holds (x, y, z, input id bits); the component labels are
+            // read beside it from lab
             auto scan_leaf = [&](uint32_t leaf) {
                 const uint32_t b = leaf * 32;
                 if (b >= n) return;  // padding leaf (never reached: its bound is +inf)
                 const uint32_t m = min(32u, n - b);
                 ++st_leaves;
                 st_cands += m;
-                const float own = __uint_as_float(labp);
                 // a leaf straddling clouds: check every candidate's cloud
                 bool mixed = false;
                 if constexpr (CL) {
@@ -153,26 +129,23 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 }
                 for (uint32_t j = 0; j < m; j += 4) {
                     float4 c[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        c[k] = j + k < m ? __ldg(&spl[b + j + k]) : make_float4(0.f, 0.f, 0.f, own);
+                    uint32_t cl[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        if (__float_as_uint(c[k].w) == labp) continue;
+                        c[k] = j + k < m ? __ldg(&sp[b + j + k]) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        cl[k] = j + k < m ? __ldg(&lab[b + j + k]) : labp;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (cl[k] == labp) continue;
                         if (CL && mixed && j + k < m && __ldg(&pcloud[b + j + k]) != qc) continue;
                         const float d2 =
                             d2_of<D>(__fsub_rn(c[k].x, P.x), __fsub_rn(c[k].y, P.y), __fsub_rn(c[k].z, P.z));
-                        if (d2 < bd) {
+                        const int oq = __float_as_int(c[k].w);
+                        if (d2 < bd || (d2 == bd && oq < bo)) {
                             bd = d2;
+                            bo = oq;
                             bs = (int)(b + j + k);
-                            bo = -1;
-                        } else if (d2 == bd) {
-                            const int oq = (int)__ldg(&perm[b + j + k]);
-                            if (bo < 0) bo = (int)__ldg(&perm[bs]);
-                            if (oq < bo) {
-                                bo = oq;
-                                bs = (int)(b + j + k);
-                            }
                         }
                     }
                 }
@@ -207,11 +180,8 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 ++st_nodes;
                 const float ls = node_lb(sib);
                 if (!(ls < INFINITY)) continue;
-                if (ls > fminf(fminf(bd, cb), cap)) {
-                    if (ls <= bd) {
-                        cut = fminf(cut, ls);
-                        if (LEARN && ls <= cb) capped = true;
-                    }
+                if (ls > fminf(bd, cb)) {
+                    if (ls <= bd) cut = fminf(cut, ls);
                     continue;
                 }
                 int top = 0;
@@ -229,9 +199,8 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                             // bound re-checked: bd may have shrunk since the push
                             const float lb = node_lb(node);
                             if (!(lb < INFINITY) || lb > bd) continue;
-                            if (lb > fminf(cb, cap)) {
+                            if (lb > cb) {
                                 cut = fminf(cut, lb);
-                                if (LEARN && lb <= cb) capped = true;
                                 continue;
                             }
                             leaf = node - L;
@@ -239,7 +208,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                         }
                         const uint32_t c0 = 2 * node, c1 = c0 + 1;
                         const float l0 = node_lb(c0), l1 = node_lb(c1);
-                        const float lim = fminf(fminf(bd, cb), cap);
+                        const float lim = fminf(bd, cb);
                         // push the farther child first so the nearer one is searched next
                         const bool near0 = l0 <= l1;
                         const uint32_t cn = near0 ? c0 : c1, cf = near0 ? c1 : c0;
@@ -249,15 +218,9 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                             break;
                         }
                         if (lf < INFINITY && lf <= lim) stack[top++] = cf;
-                        else if (lf <= bd && lf < INFINITY) {
-                            cut = fminf(cut, lf);
-                            if (LEARN && lf <= cb) capped = true;
-                        }
+                        else if (lf <= bd && lf < INFINITY) cut = fminf(cut, lf);
                         if (ln < INFINITY && ln <= lim) stack[top++] = cn;
-                        else if (ln <= bd && ln < INFINITY) {
-                            cut = fminf(cut, ln);
-                            if (LEARN && ln <= cb) capped = true;
-                        }
+                        else if (ln <= bd && ln < INFINITY) cut = fminf(cut, ln);
                     }
                     if (leaf != kNone) {
                         scan_leaf(leaf);
@@ -267,23 +230,15 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 }
             }
             const bool exact = bs >= 0 && bd < cut;
-            // nodes left out only by the radius may hold a closer point: search
-            // again in the second pass (the lower bound below stays valid)
-            again = capped && !exact;
             lbp[me] = exact ? bd : fmaxf(lb0, fminf(cut, bd));
             if (bs >= 0) {
-                if (bo < 0) bo = (int)__ldg(&perm[bs]);
                 const uint32_t mn = (uint32_t)min(op, bo);
                 const uint64_t key = ((uint64_t)__float_as_uint(bd) << 32) | mn;
                 selq[me] = exact ? (uint32_t)bs : kNone;
                 selkey[me] = key;
                 if (key <= __ldcg(&ckey[labp])) {
                     const uint64_t old = atomicMin((unsigned long long*)&ckey[labp], (unsigned long long)key);
-                    // a result the second pass will redo still bounds the
-                    // component's key, but only its second search may list
-                    // the point as a provisional winner (at most once a round:
-                    // the list holds n entries)
-                    record = old >= key && !again;
+                    record = old >= key;
                 }
             } else {
                 selq[me] = kNone;
@@ -293,8 +248,7 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
         // lanes of a diverged warp drift into different iterations and the
         // next traversals run with a fraction of the warp active.
         __syncwarp();
-        // second-pass candidates (2), compacted in leaf order after the first pass
-        if (listed && pass == 1) dflag[me] = (deferred || again) ? 2 : 0;
+        if (listed && pass == 1) dflag[me] = 0;
         warp_append(record, me, prov, n_prov);
         if (stats) {
             unsigned long long sl = st_leaves, sn = st_nodes, sc = st_cands, q = valid ? 1ull : 0ull;
@@ -305,8 +259,6 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 q += __shfl_xor_sync(kFull, q, o);
             }
             const unsigned first = __ballot_sync(kFull, valid && pass == 1);
-            const unsigned resumed = __ballot_sync(kFull, again);
-            const unsigned later = __ballot_sync(kFull, deferred);
             if ((threadIdx.x & 31) == 0) {
                 atomicAdd(&stats[0], sl);
                 atomicAdd(&stats[1], sn);
@@ -314,8 +266,6 @@ __global__ void __launch_bounds__(TPB, MINB) k_cnns_t(const CnnsArgs a)
                 atomicAdd(&stats[3], 1ull);
                 atomicAdd(&stats[4], q);
                 atomicAdd(&stats[5], (unsigned long long)__popc(first));
-                atomicAdd(&stats[6], (unsigned long long)__popc(resumed));
-                atomicAdd(&stats[7], (unsigned long long)__popc(later));
             }
         }
     }
@@ -342,8 +292,8 @@ __global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
     const uint32_t n1 = *a.n_list;
     const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
     if (total > a.wide_limit) return;  // a long list: k_cnns_t's
-    const float4* __restrict__ spl = a.spl;
-    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ sp = a.sp;
+    const uint32_t* __restrict__ lab = a.lab;
     const float4* __restrict__ nlo = a.nlo;
     const float4* __restrict__ nhi = a.nhi;
     const uint32_t* __restrict__ nlab = a.nlab;
@@ -380,8 +330,8 @@ __global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
         uint32_t st_leaves = 0, st_nodes = 0;
         bool record = false;
         if (valid) {
-            const float4 P = spl[me];
-            const uint32_t op = __ldg(&perm[me]);
+            const float4 P = sp[me];
+            const uint32_t op = __float_as_uint(P.w);
             const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
             float bd = INFINITY, cut = INFINITY;
             uint64_t bkey = ~0ull;  // best: d2 bits << 32 | input id
@@ -409,13 +359,13 @@ __global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
                 ++st_leaves;
                 uint32_t kd = ~0u, ki = ~0u;
                 if ((uint32_t)lane < m) {
-                    const float4 c = __ldg(&spl[b + lane]);
-                    bool ok = __float_as_uint(c.w) != labp;
+                    const float4 c = __ldg(&sp[b + lane]);
+                    bool ok = __ldg(&lab[b + lane]) != labp;
                     if constexpr (CL) ok = ok && __ldg(&pcloud[b + lane]) == qc;
                     if (ok) {
                         kd = __float_as_uint(
                             d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z)));
-                        ki = __ldg(&perm[b + lane]);
+                        ki = __float_as_uint(c.w);
                     }
                 }
                 // non-negative floats order as their bits
@@ -568,8 +518,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     const uint32_t n1 = *a.n_list;
     const uint32_t total = n1 + (a.list2 ? *a.n_list2 : 0u);
     if (total <= a.wide_limit || total <= a.coop_min) return;  // shorter lists: k_cnns_w, k_cnns_t
-    const float4* __restrict__ spl = a.spl;
-    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ sp = a.sp;
+    const uint32_t* __restrict__ lab = a.lab;
     const float4* __restrict__ nlo = a.nlo;
     const float4* __restrict__ nhi = a.nhi;
     const uint32_t* __restrict__ nlab = a.nlab;
@@ -579,12 +529,12 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     uint64_t* __restrict__ ckey = a.ckey;
     constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
     __shared__ float4 s_pt[kKnnWarps][32];
-    __shared__ uint32_t s_id[kKnnWarps][32];
+    __shared__ uint32_t s_lab[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const pt = s_pt[w];
-    uint32_t* const ids = s_id[w];
+    uint32_t* const labs = s_lab[w];
     uint32_t* const stack = s_stack[w];
     const uint32_t stride = gridDim.x * kKnnWarps * 32;
     for (uint32_t base0 = (blockIdx.x * kKnnWarps + w) * 32; base0 < total; base0 += stride) {
@@ -603,8 +553,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
         };
         refresh_cb();
         const bool valid = listed && !(lb0 > cb);  // else it cannot hold its component's minimum this round
-        const float4 P = spl[me];
-        const uint32_t op = __ldg(&perm[me]);
+        const float4 P = sp[me];
+        const uint32_t op = __float_as_uint(P.w);
         const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
         // best d2 so far (+inf: none); -1 for lanes with no search, so that
         // no node and no candidate is ever theirs
@@ -642,13 +592,13 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
             ++st_leaves;
             __syncwarp();  // the previous leaf's reads are done
             if ((uint32_t)lane < m) {
-                pt[lane] = __ldg(&spl[b + lane]);
-                ids[lane] = __ldg(&perm[b + lane]);
+                pt[lane] = __ldg(&sp[b + lane]);
+                labs[lane] = __ldg(&lab[b + lane]);
                 if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
             } else {
                 // past the last point: NaN coordinates fail every d2 <= bound test
-                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(kEmpty));
-                ids[lane] = ~0u;
+                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(~0u));
+                labs[lane] = kEmpty;
                 if constexpr (CL) s_cl[w][lane] = ~0u;
             }
             __syncwarp();
@@ -657,9 +607,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
                 for (int j = 0; j < 32; ++j) {
                     const float4 c = pt[j];
                     const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                    bool ok = d2 <= bd && __float_as_uint(c.w) != labp;
+                    bool ok = d2 <= bd && labs[j] != labp;
                     if constexpr (CL) ok = ok && s_cl[w][j] == qc;
-                    const uint32_t id = ids[j];
+                    const uint32_t id = __float_as_uint(c.w);
                     const bool better = ok && (d2 < bd || id < bo);  // (d2, id) order; ok has d2 <= bd
                     bd = better ? d2 : bd;
                     bo = better ? id : bo;
@@ -667,7 +617,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
                 }
             } else {
                 const float4 c = pt[lane];
-                const uint32_t cid = ids[lane];
+                const uint32_t cid = __float_as_uint(c.w);
+                const uint32_t clab = labs[lane];
                 const uint32_t cc = CL ? s_cl[w][lane] : 0u;
                 while (need) {
                     const int q = __ffs(need) - 1;
@@ -679,7 +630,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
                     const uint32_t ql = __shfl_sync(kFull, labp, q);
                     const uint32_t qq = CL ? __shfl_sync(kFull, qc, q) : 0u;
                     const float d2 = d2_of<D>(__fsub_rn(c.x, qx), __fsub_rn(c.y, qy), __fsub_rn(c.z, qz));
-                    bool ok = d2 <= qb && __float_as_uint(c.w) != ql;
+                    bool ok = d2 <= qb && clab != ql;
                     if constexpr (CL) ok = ok && cc == qq;
                     const uint32_t kd = ok ? __float_as_uint(d2) : ~0u;  // non-negative floats order as bits
                     const uint32_t md = __reduce_min_sync(kFull, kd);
@@ -798,14 +749,13 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
 // the exact K nearest, as with one traversal per lane.  During the search a
 // list holds only its (d2 bits, input id) keys; each entry's leaf position is
 // read from iperm (input id -> position) once, when the list is written.
-template <int D, bool CL>
+template <int D, bool CL, bool LEARN>
 __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ klist,
                                                                 unsigned char* __restrict__ kcur,
                                                                 const uint32_t* __restrict__ iperm)
 {
     if (*a.round != 1) return;
-    const float4* __restrict__ spl = a.spl;
-    const uint32_t* __restrict__ perm = a.perm;
+    const float4* __restrict__ sp = a.sp;
     const float4* __restrict__ nlo = a.nlo;
     const float4* __restrict__ nhi = a.nhi;
     const uint32_t n = a.n, L = a.L;
@@ -813,12 +763,10 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     const uint32_t* __restrict__ ncloud = a.ncloud;
     constexpr int K = kKnn, kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
     __shared__ float4 s_pt[kKnnWarps][32];
-    __shared__ uint32_t s_id[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const pt = s_pt[w];
-    uint32_t* const ids = s_id[w];
     uint32_t* const stack = s_stack[w];
     const uint32_t total = *a.n_list;
     const uint32_t stride = gridDim.x * kKnnWarps * 32;
@@ -826,8 +774,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         const uint32_t qi = base0 + lane;
         const bool listed = qi < total;
         const uint32_t me = a.list[listed ? qi : base0];
-        const uint32_t labp = listed ? a.lab[me] : kEmpty;
-        const float4 P = spl[me];
+        const float4 P = sp[me];
         const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
         // the list: (d2 bits << 32 | input id), sorted; positions are looked
         // up from the ids once at the end
@@ -839,7 +786,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         // lanes past the list's end take -1 so that no node and no candidate
         // is ever theirs
         float bd = listed ? FLT_MAX : -1.f;
-        uint32_t st_leaves = 0, st_nodes = 0;
+        uint32_t st_leaves = 0, st_nodes = 0, st_marked = 0, st_steps = 0;
 
         // This lane's lower bound of d2 over a node's box.  An empty box
         // (lo = +inf, hi = -inf) gives +inf through the arithmetic.  Node
@@ -867,21 +814,23 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         // (one ballot per query).  A lane that does not want the leaf has no
         // point in it within its bound (the box bound never exceeds a
         // point's d2: both round the same differences the same way).
-        auto scan_leaf = [&](uint32_t leaf, uint32_t need) {
-            const uint32_t b = leaf * 32;
-            const uint32_t m = min(32u, n - b);
-            ++st_leaves;
+        auto stage_leaf = [&](uint32_t b, uint32_t m) {
             __syncwarp();  // the previous leaf's reads are done
             if ((uint32_t)lane < m) {
-                pt[lane] = __ldg(&spl[b + lane]);
-                ids[lane] = __ldg(&perm[b + lane]);
+                pt[lane] = __ldg(&sp[b + lane]);
                 if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
             } else {
                 // past the last point: NaN coordinates fail every d2 <= bound test
-                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(labp));
+                pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);
                 if constexpr (CL) s_cl[w][lane] = ~0u;
             }
             __syncwarp();
+        };
+        auto scan_leaf = [&](uint32_t leaf, uint32_t need, bool staged) {
+            const uint32_t b = leaf * 32;
+            const uint32_t m = min(32u, n - b);
+            ++st_leaves;
+            if (!staged) stage_leaf(b, m);
             uint32_t mask = 0;
             if (__popc(need) > kKnnDense) {
 #pragma unroll
@@ -905,23 +854,26 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                     const float qx = __shfl_sync(kFull, P.x, q), qy = __shfl_sync(kFull, P.y, q);
                     const float qz = D == 3 ? __shfl_sync(kFull, P.z, q) : 0.f;
                     const float qb = __shfl_sync(kFull, bd, q);
-                    const uint32_t ql = __shfl_sync(kFull, labp, q);
+                    // round 1: the query's component is the query alone
+                    const uint32_t qme = __shfl_sync(kFull, me, q);
                     // every lane takes part in every shuffle (none under a condition)
                     const uint32_t qq = CL ? __shfl_sync(kFull, qc, q) : 0u;
                     const float d2 = d2_of<D>(__fsub_rn(c.x, qx), __fsub_rn(c.y, qy), __fsub_rn(c.z, qz));
-                    bool ok = d2 <= qb && __float_as_uint(c.w) != ql;
+                    bool ok = d2 <= qb && b + (uint32_t)lane != qme;
                     if constexpr (CL) ok = ok && cc == qq;
                     const uint32_t mb = __ballot_sync(kFull, ok);
                     if (lane == q) mask = mb;
                 }
             }
+            st_marked += __popc(mask);
             while (mask) {
                 const int j = __ffs(mask) - 1;
                 mask &= mask - 1u;
+                ++st_steps;
                 const float4 c = pt[j];
                 const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
                 if (d2 > bd) continue;
-                const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | ids[j];
+                const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | __float_as_uint(c.w);
                 if (key >= kk[K - 1]) continue;
                 // sorted insert, all in registers
 #pragma unroll
@@ -938,34 +890,135 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         // the warp's own leaf (lane 0's query's) first, then bottom-up: every
         // other leaf lies in exactly one sibling subtree of its ancestors
         const uint32_t own = __shfl_sync(kFull, me, 0) >> 5;
-        scan_leaf(own, __ballot_sync(kFull, bd >= 0.f));
-        for (uint32_t v = L + own; v > 1; v >>= 1) {
-            const uint32_t sib = v ^ 1u;
-            ++st_nodes;
-            if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
-            int top = 0;
-            stack[top++] = sib;
-            while (top > 0) {
-                const uint32_t node = stack[--top];
-                ++st_nodes;
-                if (node >= L) {
-                    // bounds re-checked: they may have shrunk since the push
-                    const uint32_t need = __ballot_sync(kFull, wanted(node_lb(node)));
-                    if (need) scan_leaf(node - L, need);
-                    continue;
+        float tk = INFINITY;   // the own leaf's certified bound
+        bool guessed = false;  // the walk starts from the learned radius, below tk
+        float f[prop::kIn];    // proposal features (learned bound, traces)
+        const bool tracing = a.trace != nullptr;
+        {
+            // Each lane's bound before the walk: the K-th smallest d2 to the
+            // other points of the warp's own leaf (a min/max network over K
+            // floats, no ids), an upper bound of its K-th nearest distance.
+            // Marked with it instead of FLT_MAX, the own leaf and the leaves
+            // after it offer only points that can still make the list, so
+            // far fewer inserts run; a leaf of fewer than K + 1 points leaves
+            // FLT_MAX.
+            const uint32_t m_own = min(32u, n - own * 32);
+            stage_leaf(own * 32, m_own);
+            const int self = (me >> 5) == own ? (int)(me & 31u) : -1;
+            float t[K];
+#pragma unroll
+            for (int i = 0; i < K; ++i) t[i] = INFINITY;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float4 c = pt[j];
+                float d = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                bool ok = j != self && d <= FLT_MAX;  // NaN padding and the query itself are out
+                if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                d = ok ? d : INFINITY;
+#pragma unroll
+                for (int i = 0; i < K; ++i) {
+                    const float lo = fminf(t[i], d);
+                    d = fmaxf(t[i], d);
+                    t[i] = lo;
                 }
-                const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                const float l0 = node_lb(c0), l1 = node_lb(c1);
-                const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
-                // the child nearer to the warp's nearest lane is searched next
-                const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
-                const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
-                const bool near0 = m0 <= m1;
-                const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
-                __syncwarp();  // every lane has read the popped entry
-                if (wf) stack[top++] = near0 ? c1 : c0;
-                if (wn) stack[top++] = near0 ? c0 : c1;
-                __syncwarp();
+            }
+            tk = t[K - 1];
+            if (listed && tk < bd) bd = tk;
+            if (LEARN || tracing) {
+                const bool fin = listed && tk < INFINITY;
+                const uint32_t ol = L + (me >> 5);
+                const float4 lo = __ldg(&nlo[ol]), hi = __ldg(&nhi[ol]);
+                const float4 plo = __ldg(&nlo[ol >> 1]), phi = __ldg(&nhi[ol >> 1]);
+                const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = D == 3 ? hi.z - lo.z : 0.f;
+                const float px = phi.x - plo.x, py = phi.y - plo.y, pz = D == 3 ? phi.z - plo.z : 0.f;
+                float e = fminf(fminf(P.x - lo.x, hi.x - P.x), fminf(P.y - lo.y, hi.y - P.y));
+                if (D == 3) e = fminf(e, fminf(P.z - lo.z, hi.z - P.z));
+                if (fin) {
+                    prop::knn_features(t[0], t[2], tk, ex * ex + ey * ey + ez * ez, e * e,
+                                       px * px + py * py + pz * pz, (float)min(32u, n - (me >> 5) * 32) * (1.f / 32.f),
+                                       1, 1.f, f);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < prop::kIn; ++i) f[i] = 0.f;
+                }
+                if constexpr (LEARN) {
+                    // one tensor-core inference for the warp's 32 queries
+                    float o0, o1;
+                    prop::infer_warp(reinterpret_cast<const prop::Frag*>(a.frag), f, o0, o1);
+                    if (fin && o1 >= a.threshold) {
+                        const float r = tk * exp2f(fminf(fmaf(8.f, o0, a.margin), 0.f));
+                        if (r < bd) {
+                            bd = r;
+                            guessed = true;
+                        }
+                    }
+                }
+            }
+        }
+        const bool learned_lane = guessed;
+        bool resumed = false;
+        for (int attempt = 0;; ++attempt) {
+            scan_leaf(own, __ballot_sync(kFull, bd >= 0.f), attempt == 0);
+            for (uint32_t v = L + own; v > 1; v >>= 1) {
+                const uint32_t sib = v ^ 1u;
+                ++st_nodes;
+                if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
+                int top = 0;
+                stack[top++] = sib;
+                while (top > 0) {
+                    const uint32_t node = stack[--top];
+                    ++st_nodes;
+                    if (node >= L) {
+                        // bounds re-checked: they may have shrunk since the push
+                        const uint32_t need = __ballot_sync(kFull, wanted(node_lb(node)));
+                        if (need) scan_leaf(node - L, need, false);
+                        continue;
+                    }
+                    const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                    const float l0 = node_lb(c0), l1 = node_lb(c1);
+                    const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
+                    // the child nearer to the warp's nearest lane is searched next
+                    const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
+                    const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
+                    const bool near0 = m0 <= m1;
+                    const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
+                    __syncwarp();  // every lane has read the popped entry
+                    if (wf) stack[top++] = near0 ? c1 : c0;
+                    if (wn) stack[top++] = near0 ? c0 : c1;
+                    __syncwarp();
+                }
+            }
+            if constexpr (!LEARN) break;
+            // A learned radius that held fewer than K points: the list is not
+            // the K nearest.  Those lanes start over from the certified
+            // bound; the others sit the walk out (bound -1: they want nothing).
+            const bool miss = guessed && kk[K - 1] == kNoKey;
+            if (attempt > 0 || !__any_sync(kFull, miss)) break;
+            if (miss) {
+#pragma unroll
+                for (int j = 0; j < K; ++j) kk[j] = kNoKey;
+                bd = tk;
+                resumed = true;
+            } else {
+                bd = -1.f;
+            }
+            guessed = false;
+        }
+        if (tracing && listed && tk < INFINITY && (knn_sample_hash(me) & a.trace_mask) == 0) {
+            // training record: features, the target radius log2(d2 of the
+            // K-th nearest / tk) / 8, whether tk could be tightened at all,
+            // the regression mask (the list is full)
+            const uint32_t at = atomicAdd(a.trace_ctl, 1u);
+            if (at < a.trace_cap) {
+                float* o = a.trace + (uint64_t)at * prop::kRec;
+                const bool full = kk[K - 1] != kNoKey;
+                const float rk = full ? __uint_as_float((uint32_t)(kk[K - 1] >> 32)) : tk;
+#pragma unroll
+                for (int i = 0; i < prop::kIn; ++i) o[i] = f[i];
+                o[8] = full ? prop::lg8(rk) - prop::lg8(tk) : 0.f;
+                o[9] = full && rk < tk ? 1.f : 0.f;
+                o[10] = full ? 1.f : 0.f;
+                o[11] = 0.f;
             }
         }
         uint32_t p0 = kNone;  // entry 0's leaf position
@@ -982,7 +1035,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         // distance was searched)
         bool record = false;
         if (listed) {
-            const int op = (int)__ldg(&perm[me]);
+            const int op = __float_as_int(P.w);
             if (kk[0] != kNoKey) {
                 const float d0 = __uint_as_float((uint32_t)(kk[0] >> 32));
                 const uint32_t mn = (uint32_t)min(op, (int)(uint32_t)kk[0]);
@@ -990,10 +1043,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 a.lbp[me] = d0;
                 a.selq[me] = p0;
                 a.selkey[me] = key;
-                if (key <= __ldcg(&a.ckey[labp])) {
-                    const uint64_t old = atomicMin((unsigned long long*)&a.ckey[labp], (unsigned long long)key);
-                    record = old >= key;
-                }
+                // round 1: every point is its own component, the only writer of its key
+                a.ckey[me] = key;
+                record = true;
             } else {
                 a.lbp[me] = INFINITY;  // alone in its cloud
                 a.selq[me] = kNone;
@@ -1002,8 +1054,12 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         __syncwarp();
         warp_append(record, me, a.prov, a.n_prov);
         if (a.stats) {
-            // leaves and nodes are per warp; candidates per listed lane
+            // leaves, nodes and insert steps are per warp; candidates per listed lane
             unsigned long long q = __popc(__ballot_sync(kFull, listed));
+            const uint32_t marked = __reduce_add_sync(kFull, st_marked);
+            const uint32_t steps = __reduce_max_sync(kFull, st_steps);
+            const uint32_t nl = __popc(__ballot_sync(kFull, learned_lane));
+            const uint32_t nr = __popc(__ballot_sync(kFull, resumed));
             if (lane == 0) {
                 atomicAdd(&a.stats[0], (unsigned long long)st_leaves);
                 atomicAdd(&a.stats[1], (unsigned long long)st_nodes * 32ull);
@@ -1011,6 +1067,10 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 atomicAdd(&a.stats[3], 1ull);
                 atomicAdd(&a.stats[4], q);
                 atomicAdd(&a.stats[5], q);
+                atomicAdd(&a.stats[8], (unsigned long long)marked);
+                atomicAdd(&a.stats[9], (unsigned long long)steps);
+                atomicAdd(&a.stats[10], (unsigned long long)nl);
+                atomicAdd(&a.stats[11], (unsigned long long)nr);
             }
         }
     }
@@ -1019,7 +1079,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
 
 // Launch of one shape; the grid covers the list's upper bound `a.n` with at
 // most four waves of resident blocks (the kernel strides over the rest).
-template <int D, bool CL, int I, bool LEARN>
+template <int D, bool CL, int I>
 void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
 {
     constexpr int T = kSearchShapes[I].threads, M = kSearchShapes[I].min_blocks;
@@ -1027,10 +1087,10 @@ void launch_shape(const CnnsArgs& a, int sms, cudaStream_t s)
     const uint64_t cap = (uint64_t)sms * M * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_cnns_t<D, CL, T, M, LEARN><<<(unsigned)b, T, 0, s>>>(a);
+    k_cnns_t<D, CL, T, M><<<(unsigned)b, T, 0, s>>>(a);
 }
 
-template <int D, bool CL>
+template <int D, bool CL, bool LEARN>
 cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, const uint32_t* iperm, int sms,
                        cudaStream_t s)
 {
@@ -1039,21 +1099,21 @@ cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, 
     const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm);
+    k_knn_first<D, CL, LEARN><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm);
     return cudaGetLastError();
 }
 
-template <int D, bool CL, bool LEARN = false>
+template <int D, bool CL>
 cudaError_t launch_dim(const CnnsArgs& a, int shape, int sms, cudaStream_t s)
 {
     static_assert(kNumSearchShapes == 6, "one case per shape");
     switch (shape) {
-    case 0: launch_shape<D, CL, 0, LEARN>(a, sms, s); break;
-    case 1: launch_shape<D, CL, 1, LEARN>(a, sms, s); break;
-    case 2: launch_shape<D, CL, 2, LEARN>(a, sms, s); break;
-    case 3: launch_shape<D, CL, 3, LEARN>(a, sms, s); break;
-    case 4: launch_shape<D, CL, 4, LEARN>(a, sms, s); break;
-    case 5: launch_shape<D, CL, 5, LEARN>(a, sms, s); break;
+    case 0: launch_shape<D, CL, 0>(a, sms, s); break;
+    case 1: launch_shape<D, CL, 1>(a, sms, s); break;
+    case 2: launch_shape<D, CL, 2>(a, sms, s); break;
+    case 3: launch_shape<D, CL, 3>(a, sms, s); break;
+    case 4: launch_shape<D, CL, 4>(a, sms, s); break;
+    case 5: launch_shape<D, CL, 5>(a, sms, s); break;
     default: return cudaErrorInvalidValue;
     }
     if (a.wide_limit > 0) {

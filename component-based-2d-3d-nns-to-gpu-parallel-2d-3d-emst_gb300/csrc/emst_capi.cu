@@ -181,12 +181,14 @@ emst_status do_octants(emst_ctx* x)
     c.round++;
     Timed t(x, PH_OCTANTS);
     EMST_CUDA(x, emst::round_tick(c), "round tick");
-    if (c.search_mode == 0)
-        EMST_CUDA(x, emst::cnns_node_labels(c), "compute_octants (node labels)");
-    else if (c.round == 1)
-        EMST_CUDA(x, emst::nns_full(c), "compute_octants");
-    else
-        EMST_CUDA(x, emst::nns_recompute_zero(c), "compute_octants (zero recompute)");
+    // (component search: nothing to do here -- the node labels it prunes with
+    // were written by the last flatten, or by the initialisation before round 1)
+    if (c.search_mode != 0) {
+        if (c.round == 1)
+            EMST_CUDA(x, emst::nns_full(c), "compute_octants");
+        else
+            EMST_CUDA(x, emst::nns_recompute_zero(c), "compute_octants (zero recompute)");
+    }
     x->stage = 2;
     return EMST_OK;
 }
@@ -261,7 +263,7 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     if (n >= (int64_t)0x7fffffff) return set_err(x, EMST_EOVERFLOW, "n must be < 2^31 - 1");
     EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
     if (!is_device) {
-        EMST_CUDA(x, emst::ensure(c.in_own, (size_t)n * dim), "alloc points");
+        EMST_CUDA(x, c.ensure(c.in_own, (size_t)n * dim), "alloc points");
         EMST_CUDA(x, cudaMemcpyAsync(c.in_own.p, points, sizeof(float) * n * dim, cudaMemcpyHostToDevice, c.stream),
                   "upload points");
         c.in = c.in_own.p;
@@ -284,12 +286,12 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
     c.knn_timed = 0;
     c.search_timed = 0;
     if (c.profile) {
-        EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
-        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), c.stream), "stats");
+        EMST_CUDA(x, c.ensure(c.nstats, emst::kNumStats), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, emst::kNumStats * sizeof(unsigned long long), c.stream), "stats");
     }
     c.snap_cap = 0;
     if (c.snap_rounds > 0) {
-        EMST_CUDA(x, emst::ensure(c.snaps, (size_t)c.snap_rounds * n), "alloc snapshots");
+        EMST_CUDA(x, c.ensure(c.snaps, (size_t)c.snap_rounds * n), "alloc snapshots");
         c.snap_cap = c.snap_rounds;
     }
     for (double& v : x->ms) v = 0.0;
@@ -324,7 +326,6 @@ emst_status enqueue_round(emst_ctx* x, cudaGraphConditionalHandle h)
 {
     Ctx& c = x->c;
     EMST_CUDA(x, emst::round_tick(c), "round tick");
-    EMST_CUDA(x, emst::cnns_node_labels(c), "node labels");
     EMST_CUDA(x, emst::cnns_select(c), "find_next_closest");
     EMST_CUDA(x, emst::boruvka_resolve(c), "find_min_pair");
     EMST_CUDA(x, emst::boruvka_hook(c), "connect_union");
@@ -342,8 +343,8 @@ emst_status build_graph(emst_ctx* x)
 {
     Ctx& c = x->c;
     std::vector<const void*> key = {(const void*)(intptr_t)c.n, (const void*)(intptr_t)c.dim, c.in, c.sp.p,
-                                    c.spl.p,  c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
-                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p, c.dflag.p, c.sel_tmp.p,
+                                    c.lab.p, c.roots.p, c.edges.p, c.nlab.p, c.lbp.p, c.prov.p,
+                                    c.dirty.p, c.perm.p, c.selq.p, c.ckey.p, c.nlo.p, c.dflag.p,
                                     (const void*)(intptr_t)emst::search_shape_of(c), c.pfrag.p,
                                     (const void*)(intptr_t)(c.learned ? 1 : 0), c.trace.p,
                                     (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
@@ -467,8 +468,8 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
     cudaError_t e = cudaSetDevice(c.device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, c.device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = emst::ensure(c.ctr, 1);
-    if (e == cudaSuccess) e = emst::ensure(c.dlen, 1);
+    if (e == cudaSuccess) e = c.ensure(c.ctr, 1);
+    if (e == cudaSuccess) e = c.ensure(c.dlen, 1);
     if (e == cudaSuccess) e = cudaMallocHost(&c.hctr, sizeof(emst::DevCounters));
     if (e == cudaSuccess) e = cudaMallocHost(&c.hlen, sizeof(double));
     if (e != cudaSuccess) {
@@ -505,6 +506,7 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.dirty);
     emst::release(c.dirty2);
     emst::release(c.dflag);
+    emst::release(c.sel_tiles);
     emst::release(c.pfrag);
     emst::release(c.trace);
     emst::release(c.trace_ctl);
@@ -512,10 +514,8 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.klist);
     emst::release(c.iperm);
     emst::release(c.kcur);
-    emst::release(c.sel_tmp);
     emst::release(c.lbp);
     emst::release(c.clb);
-    emst::release(c.spl);
     emst::release(c.d_off);
     emst::release(c.d_foff);
     emst::release(c.d_eoff);
@@ -677,7 +677,7 @@ emst_status emst_get_labels(emst_ctx* x, int32_t* labels, int64_t cap)
     if (st != EMST_OK) return st;
     Ctx& c = x->c;
     if (!labels || cap < c.n) return set_err(x, EMST_EOVERFLOW, "labels buffer too small");
-    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)c.n), "alloc");
+    EMST_CUDA(x, x->c.ensure(x->tmp_i32, (size_t)c.n), "alloc");
     EMST_CUDA(x, emst::labels_to_input_order(c, x->tmp_i32.p), "labels");
     EMST_CUDA(x, cudaMemcpyAsync(labels, x->tmp_i32.p, sizeof(int32_t) * c.n, cudaMemcpyDeviceToHost, c.stream),
               "labels");
@@ -732,8 +732,12 @@ emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
     out->octant_launches = x->c.nns_launches;
     out->rounds = x->c.round;
     if (x->c.profile && x->c.nstats.p) {
-        unsigned long long st[8];
+        unsigned long long st[emst::kNumStats];
         EMST_CUDA(x, cudaMemcpy(st, x->c.nstats.p, sizeof(st), cudaMemcpyDeviceToHost), "stats");
+        out->knn_marked = (int64_t)st[8];
+        out->knn_insert_steps = (int64_t)st[9];
+        out->knn_learned = (int64_t)st[10];
+        out->knn_resumed = (int64_t)st[11];
         out->first_pass_searches = (int64_t)st[5];
         out->first_pass_resumed = (int64_t)st[6];
         out->first_pass_deferred = (int64_t)st[7];
@@ -762,7 +766,7 @@ emst_status emst_get_round_labels(emst_ctx* x, int round, int32_t* labels, int64
     if (round < 1 || round > (int)c.cum_edges.size()) return set_err(x, EMST_EINVAL, "no such round");
     if (round > c.snap_cap) return set_err(x, EMST_EINVAL, "round labels not kept (emst_keep_round_labels)");
     if (!labels || cap < c.n) return set_err(x, EMST_EOVERFLOW, "labels buffer too small");
-    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)c.n), "alloc");
+    EMST_CUDA(x, x->c.ensure(x->tmp_i32, (size_t)c.n), "alloc");
     EMST_CUDA(x, emst::labels_to_input_order(c, x->tmp_i32.p, c.snaps.p + (size_t)(round - 1) * c.n), "labels");
     EMST_CUDA(x, cudaMemcpyAsync(labels, x->tmp_i32.p, sizeof(int32_t) * c.n, cudaMemcpyDeviceToHost, c.stream),
               "labels");
@@ -841,13 +845,13 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
         for (int i = 0; lengths && i < n_clouds; ++i) lengths[i] = 0.0;
         return EMST_OK;
     }
-    EMST_CUDA(x, emst::ensure(c.in_own, (size_t)foff[n_clouds]), "alloc points");
-    EMST_CUDA(x, emst::ensure(c.d_off, (size_t)n_clouds + 1), "alloc");
-    EMST_CUDA(x, emst::ensure(c.d_foff, (size_t)n_clouds + 1), "alloc");
-    EMST_CUDA(x, emst::ensure(c.d_eoff, (size_t)n_clouds + 1), "alloc");
-    EMST_CUDA(x, emst::ensure(c.d_dims, (size_t)n_clouds), "alloc");
-    EMST_CUDA(x, emst::ensure(c.dlen, (size_t)n_clouds), "alloc");
-    EMST_CUDA(x, emst::ensure(x->tmp_i32, (size_t)2 * (eoff[n_clouds] > 0 ? eoff[n_clouds] : 1)), "alloc");
+    EMST_CUDA(x, c.ensure(c.in_own, (size_t)foff[n_clouds]), "alloc points");
+    EMST_CUDA(x, c.ensure(c.d_off, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, c.ensure(c.d_foff, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, c.ensure(c.d_eoff, (size_t)n_clouds + 1), "alloc");
+    EMST_CUDA(x, c.ensure(c.d_dims, (size_t)n_clouds), "alloc");
+    EMST_CUDA(x, c.ensure(c.dlen, (size_t)n_clouds), "alloc");
+    EMST_CUDA(x, x->c.ensure(x->tmp_i32, (size_t)2 * (eoff[n_clouds] > 0 ? eoff[n_clouds] : 1)), "alloc");
     cudaStream_t s = c.stream;
     EMST_CUDA(x, cudaMemcpyAsync(c.in_own.p, points, sizeof(float) * foff[n_clouds], cudaMemcpyHostToDevice, s),
               "upload");
@@ -876,8 +880,8 @@ emst_status emst_solve_batch(emst_ctx* x, const float* points, const int64_t* po
     c.search_timed = 0;
     for (double& v : x->ms) v = 0.0;
     if (c.profile) {
-        EMST_CUDA(x, emst::ensure(c.nstats, 8), "alloc");
-        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, 8 * sizeof(unsigned long long), s), "stats");
+        EMST_CUDA(x, c.ensure(c.nstats, emst::kNumStats), "alloc");
+        EMST_CUDA(x, cudaMemsetAsync(c.nstats.p, 0, emst::kNumStats * sizeof(unsigned long long), s), "stats");
     }
     {
         Timed t(x, PH_GRID);
@@ -924,8 +928,8 @@ emst_status emst_set_proposal(emst_ctx* x, const float* weights, float margin, f
     for (int i = 0; i < emst::prop::kNumWeights; ++i)
         if (!std::isfinite(weights[i])) return set_err(x, EMST_EINVAL, "non-finite proposal weight");
     EMST_CUDA(x, cudaSetDevice(c.device), "cudaSetDevice");
-    EMST_CUDA(x, emst::ensure(c.pfrag, emst::proposal_frag_bytes()), "alloc");
-    EMST_CUDA(x, emst::ensure(x->tmp_f32, (size_t)emst::prop::kNumWeights), "alloc");
+    EMST_CUDA(x, c.ensure(c.pfrag, emst::proposal_frag_bytes()), "alloc");
+    EMST_CUDA(x, x->c.ensure(x->tmp_f32, (size_t)emst::prop::kNumWeights), "alloc");
     EMST_CUDA(x, cudaMemcpyAsync(x->tmp_f32.p, weights, sizeof(float) * emst::prop::kNumWeights,
                                  cudaMemcpyHostToDevice, c.stream), "upload");
     EMST_CUDA(x, emst::proposal_pack(x->tmp_f32.p, c.pfrag.p, c.stream), "pack");
@@ -946,8 +950,8 @@ emst_status emst_trace_enable(emst_ctx* x, int64_t capacity, int sample_shift)
     c.trace_cap = capacity;
     c.trace_shift = sample_shift;
     if (capacity == 0) return EMST_OK;
-    EMST_CUDA(x, emst::ensure(c.trace, (size_t)capacity * emst::prop::kRec), "alloc trace");
-    EMST_CUDA(x, emst::ensure(c.trace_ctl, 2), "alloc");
+    EMST_CUDA(x, c.ensure(c.trace, (size_t)capacity * emst::prop::kRec), "alloc trace");
+    EMST_CUDA(x, c.ensure(c.trace_ctl, 2), "alloc");
     EMST_CUDA(x, cudaMemsetAsync(c.trace_ctl.p, 0, 2 * sizeof(uint32_t), c.stream), "trace reset");
     return EMST_OK;
 }

@@ -90,7 +90,7 @@ struct Ctx {
     DevBuf<float4> sp;
     DevBuf<uint32_t> perm, perm_alt;
     DevBuf<uint64_t> mkey, mkey_alt;
-    DevBuf<unsigned char> sort_tmp;
+    DevBuf<unsigned char> sort_tmp;  // radix sort scratch (radix_scratch_bytes)
     DevBuf<float> part;  // reduction partials
     DevBuf<NormParams> norm;
     DevBuf<float4> nlo, nhi;
@@ -131,9 +131,9 @@ struct Ctx {
     int sms = 152;            // multiprocessors of the device
     DevBuf<uint32_t> nlab;    // per node: component shared by all its points, or MIXED
     DevBuf<uint32_t> dirty, dirty2;  // points that search this round (first / second pass)
-    DevBuf<unsigned char> dflag, sel_tmp;  // per point: dirty flag; compaction scratch
+    DevBuf<unsigned char> dflag;     // per point: dirty flag (search pass)
+    DevBuf<uint32_t> sel_tiles;      // query-list compaction: per tile counts / offsets
     DevBuf<float> lbp;               // per point: lower bound of d2 to its nearest outside point
-    DevBuf<float4> spl;              // per round: (x, y, z, component label) in leaf order
 
     // batch of clouds (batch.cu)
     int n_clouds = 0;                // 0: single cloud
@@ -145,7 +145,7 @@ struct Ctx {
     DevBuf<uint32_t> ncloud;             // per node: (first cloud << 16) | last cloud of its points
     DevBuf<uint32_t> bcursor, bedges;            // output scatter cursors, edges with global ids
     DevBuf<uint32_t> clb;            // per root: min lbp over its dirty points (float bits)
-    DevBuf<unsigned long long> nstats;  // search counters (emst_profile), 8 entries
+    DevBuf<unsigned long long> nstats;  // search counters (emst_profile), kNumStats entries
 
     // learned proposal (proposal.cuh): packed weights, radius margin (log2)
     bool learned = false;
@@ -183,6 +183,12 @@ struct Ctx {
     int64_t snap_cap = 0;
     DevBuf<uint32_t> snaps;
 
+    // every buffer is carved from caller-provided memory: ensure() fails
+    // instead of allocating (the allocation-free entry point)
+    bool no_alloc = false;
+    template <typename T>
+    cudaError_t ensure(DevBuf<T>& b, size_t n);
+
     int round = 0;        // rounds started
     int phase = 0;        // 0 = not initialised, 1 = initialised
     bool finished = false;
@@ -193,6 +199,8 @@ struct Ctx {
 
 // grid.cu
 cudaError_t grid_build(Ctx& c);
+int grid_sort_end_bit(int dim);       // significant bits of the single-cloud cell keys
+int grid_reduce_blocks(int64_t n);    // blocks of the min/max reduction (partials: 6 floats each)
 cudaError_t leaf_tree(Ctx& c);
 // batch.cu
 cudaError_t batch_grid_build(Ctx& c);
@@ -217,11 +225,11 @@ cudaError_t table_to_host_order(Ctx& c);
 cudaError_t cnns_init(Ctx& c);
 cudaError_t cnns_node_labels(Ctx& c);
 cudaError_t cnns_select(Ctx& c);
-cudaError_t node_labels_of(Ctx& c, const uint32_t* labels, uint32_t* out);
+cudaError_t node_labels_of(Ctx& c, uint32_t* labels, uint32_t* out, const uint32_t* par = nullptr);
 
 // Arguments of one component-search launch (cnns_search.cuh).
 struct CnnsArgs {
-    const float4* spl;
+    const float4* sp;      // (x, y, z, input id bits) in leaf order
     const uint32_t* perm;
     const float4* nlo;
     const float4* nhi;
@@ -243,8 +251,8 @@ struct CnnsArgs {
     const uint32_t* ncloud;
     unsigned long long* stats;
     const void* frag;  // learned proposal: fragment-ordered weights (prop::Frag), or null
-    float margin;      // learned proposal: log2 margin added to the predicted radius
-    float threshold;   // learned proposal: class logit at or above which a point searches first
+    float margin;      // learned proposal: log2 factor on the predicted radius (d2)
+    float threshold;   // learned proposal: gate logit at or above which the radius is used
     const int* round;  // rounds started (device)
     const uint32_t* list2;    // second segment of the same launch (ordered first pass), or null
     const uint32_t* n_list2;
@@ -255,7 +263,19 @@ struct CnnsArgs {
     // lists longer than this (and than wide_limit) go to k_cnns_c (warp per
     // 32 queries walking together); kNoCoop: never
     uint32_t coop_min;
+    // training traces of the round-1 list build (null: off): records of
+    // prop::kRec floats, ctl[0] counts them, 1 in (mask + 1) queries sampled
+    float* trace;
+    uint32_t* trace_ctl;
+    uint64_t trace_cap;
+    uint32_t trace_mask;
 };
+
+// Search counters of profile contexts (emst_profile): 0 leaves, 1 node tests,
+// 2 candidates, 3 warps, 4 queries, 5 first-pass searches, 6 resumed, 7
+// deferred; round-1 list build: 8 candidates marked, 9 insert steps (warp),
+// 10 queries given a learned radius, 11 of those searched again.
+constexpr int kNumStats = 12;
 
 // Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
 constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
@@ -294,21 +314,23 @@ inline int search_shape_of(const Ctx& c)
 
 cudaError_t proposal_pack(const float* d_weights, void* d_frag, cudaStream_t s);
 size_t proposal_frag_bytes();
-cudaError_t proposal_trace_begin(Ctx& c);
-cudaError_t proposal_trace_end(Ctx& c);
 uint64_t splitmix(uint64_t& s);
 
-cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur,
+cudaError_t launch_knn_first2(const CnnsArgs& a, bool clouds, bool learned, uint64_t* klist, unsigned char* kcur,
                              const uint32_t* iperm, int sms, cudaStream_t s);
-cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, uint64_t* klist, unsigned char* kcur,
+cudaError_t launch_knn_first3(const CnnsArgs& a, bool clouds, bool learned, uint64_t* klist, unsigned char* kcur,
                              const uint32_t* iperm, int sms, cudaStream_t s);
-cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
-cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, bool learned, int shape, int sms, cudaStream_t s);
+cudaError_t launch_cnns_t2(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
+cudaError_t launch_cnns_t3(const CnnsArgs& a, bool clouds, int shape, int sms, cudaStream_t s);
 
+// Grows a context buffer to n elements.  A context built over caller-owned
+// memory (Ctx::no_alloc) never frees or allocates: a buffer that is too small
+// is an error, never a silent cudaMalloc.
 template <typename T>
-cudaError_t ensure(DevBuf<T>& b, size_t n)
+cudaError_t ensure(DevBuf<T>& b, size_t n, bool no_alloc)
 {
     if (b.cap >= n && b.p) return cudaSuccess;
+    if (no_alloc) return cudaErrorMemoryAllocation;
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.cap = 0;
@@ -316,6 +338,12 @@ cudaError_t ensure(DevBuf<T>& b, size_t n)
     cudaError_t e = cudaMalloc(&b.p, want * sizeof(T));
     if (e == cudaSuccess) b.cap = want;
     return e;
+}
+
+template <typename T>
+cudaError_t Ctx::ensure(DevBuf<T>& b, size_t n)
+{
+    return emst::ensure(b, n, no_alloc);
 }
 
 template <typename T>

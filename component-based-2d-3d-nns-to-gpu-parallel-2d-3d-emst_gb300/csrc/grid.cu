@@ -22,10 +22,9 @@
 #include <climits>
 #include <cmath>
 
-#include <cub/device/device_radix_sort.cuh>
-
 #include "emst_ctx.h"
 #include "emst_device.cuh"
+#include "radix.cuh"
 
 namespace emst {
 
@@ -277,28 +276,35 @@ __global__ void k_tree_level(float4* __restrict__ nlo, float4* __restrict__ nhi,
 
 }  // namespace
 
+int grid_sort_end_bit(int dim) { return dim * (dim == 3 ? kCellBits<3> : kCellBits<2>); }
+
+int grid_reduce_blocks(int64_t n)
+{
+    const int64_t b = std::min<int64_t>(kRedBlocksMax, (n + kRedThreads * 8 - 1) / (kRedThreads * 8));
+    return b < 1 ? 1 : (int)b;
+}
+
 cudaError_t grid_build(Ctx& c)
 {
     const int64_t n = c.n;
     const int D = c.dim;
     cudaStream_t s = c.stream;
     cudaError_t e;
-    int nblk = (int)std::min<int64_t>(kRedBlocksMax, (n + kRedThreads * 8 - 1) / (kRedThreads * 8));
-    if (nblk < 1) nblk = 1;
-    if ((e = ensure(c.part, (size_t)nblk * 6)) != cudaSuccess) return e;
-    if ((e = ensure(c.norm, 1)) != cudaSuccess) return e;
-    if ((e = ensure(c.scaled, (size_t)n * D)) != cudaSuccess) return e;
-    if ((e = ensure(c.mkey, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.mkey_alt, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.perm, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.perm_alt, (size_t)n)) != cudaSuccess) return e;
-    if ((e = ensure(c.sp, (size_t)n)) != cudaSuccess) return e;
+    const int nblk = grid_reduce_blocks(n);
+    if ((e = c.ensure(c.part, (size_t)nblk * 6)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.norm, 1)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.scaled, (size_t)n * D)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.mkey, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.mkey_alt, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.perm, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.perm_alt, (size_t)n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.sp, (size_t)n)) != cudaSuccess) return e;
     c.nchunk = (n + kLeaf - 1) / kLeaf;
     c.L = 1;
     while (c.L < c.nchunk) c.L <<= 1;
-    if ((e = ensure(c.nlo, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.nhi, (size_t)2 * c.L)) != cudaSuccess) return e;
-    if ((e = ensure(c.nid, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nlo, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nhi, (size_t)2 * c.L)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.nid, (size_t)2 * c.L)) != cudaSuccess) return e;
 
     if (D == 2) {
         k_minmax_part<2><<<nblk, kRedThreads, 0, s>>>(c.in, n, c.part.p, c.ctr.p);
@@ -310,17 +316,17 @@ cudaError_t grid_build(Ctx& c)
         k_rescale_key<3><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p);
     }
     // Radix sort of the cell keys (only the significant bits).
-    const int end_bit = D * (D == 3 ? kCellBits<3> : kCellBits<2>);
-    cub::DoubleBuffer<uint64_t> keys(c.mkey.p, c.mkey_alt.p);
-    cub::DoubleBuffer<uint32_t> vals(c.perm.p, c.perm_alt.p);
-    size_t tmp = 0;
-    if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp, keys, vals, (int)n, 0, end_bit, s)) != cudaSuccess)
+    const int end_bit = grid_sort_end_bit(D);
+    const size_t tmp = radix_scratch_bytes(n, end_bit);
+    if ((e = c.ensure(c.sort_tmp, tmp)) != cudaSuccess) return e;
+    bool in_alt = false;
+    if ((e = radix_sort_pairs(c.mkey.p, c.mkey_alt.p, c.perm.p, c.perm_alt.p, n, end_bit, c.sort_tmp.p, tmp,
+                              &c.ctr.p->err, &in_alt, s)) != cudaSuccess)
         return e;
-    if ((e = ensure(c.sort_tmp, tmp)) != cudaSuccess) return e;
-    if ((e = cub::DeviceRadixSort::SortPairs(c.sort_tmp.p, tmp, keys, vals, (int)n, 0, end_bit, s)) != cudaSuccess)
-        return e;
-    if (keys.Current() != c.mkey.p) std::swap(c.mkey.p, c.mkey_alt.p);
-    if (vals.Current() != c.perm.p) {
+    c.launches += 2 + radix_passes(end_bit);
+    if (in_alt) {
+        std::swap(c.mkey.p, c.mkey_alt.p);
+        std::swap(c.mkey.cap, c.mkey_alt.cap);
         std::swap(c.perm.p, c.perm_alt.p);
         std::swap(c.perm.cap, c.perm_alt.cap);
     }

@@ -353,15 +353,15 @@ cudaError_t nns_full(Ctx& c)
 {
     cudaError_t e;
     const size_t n = (size_t)c.n;
-    if ((e = ensure(c.cand, n * c.K)) != cudaSuccess) return e;
-    if ((e = ensure(c.cnt, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.cur, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.zflag, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.zero, n)) != cudaSuccess) return e;
-    if ((e = ensure(c.zero2, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.cand, n * c.K)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.cnt, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.cur, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.zflag, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.zero, n)) != cudaSuccess) return e;
+    if ((e = c.ensure(c.zero2, n)) != cudaSuccess) return e;
     if (c.keep_table) {
-        if ((e = ensure(c.tab_id, n * c.K)) != cudaSuccess) return e;
-        if ((e = ensure(c.tab_d2, n * c.K)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.tab_id, n * c.K)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.tab_d2, n * c.K)) != cudaSuccess) return e;
     }
     uint32_t* zc = &c.ctr.p->n_zero_next;
     if ((e = cudaMemsetAsync(zc, 0, sizeof(uint32_t), c.stream)) != cudaSuccess) return e;

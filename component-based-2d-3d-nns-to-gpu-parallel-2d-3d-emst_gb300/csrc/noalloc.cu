@@ -12,20 +12,29 @@
 // address: the device address is fetched once per device with
 // cudaGetSymbolAddress, with that device current, on the first call made on
 // that device, and cached.  That first call should therefore come before any
-// stream capture.
+// stream capture.  Under CUDA's lazy module loading (the default) the array
+// itself is placed on a device when this file's module is first used there,
+// which is that first call's address lookup, not the loading of the library:
+// a caller that must not see that reservation mid-run makes one call at
+// start-up.
 //
 // All calls share the array and it keeps the previous call's contents, so the
-// counters that must start at zero are cleared on every call; two calls whose
-// work overlaps on the GPU (different streams, or different host threads)
-// race on the array and must be serialised by the caller.
+// counters and sort scratch that must start at zero are cleared on every
+// call; two calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on the array and must be serialised by the
+// caller.
+//
+// The slices are sized with the same helpers the allocating path uses
+// (grid_reduce_blocks, radix_scratch_bytes), and the context is built with
+// Ctx::no_alloc set: if a slice were ever smaller than what a kernel step
+// asks for, that step fails (EMST_ENOMEM) instead of allocating.
 #include <cstring>
 #include <mutex>
-
-#include <cub/device/device_radix_sort.cuh>
 
 #include "../../include/emst.h"
 #include "emst_ctx.h"
 #include "emst_device.cuh"
+#include "radix.cuh"
 
 namespace {
 
@@ -67,6 +76,10 @@ extern "C" emst_status emst_region_table_noalloc(const float* d_points, int64_t 
     if (dim != 2 && dim != 3) return EMST_EINVAL;
     if (n < 1) return EMST_EINVAL;
     if (n > kMaxPoints) return EMST_EOVERFLOW;
+    // A launch error left pending by the caller's earlier, unrelated work is
+    // reported here, before anything is queued, rather than blamed on this
+    // call's kernels afterwards.
+    if (cudaGetLastError() != cudaSuccess) return EMST_ECUDA;
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return EMST_ECUDA;
@@ -86,6 +99,7 @@ extern "C" emst_status emst_region_table_noalloc(const float* d_points, int64_t 
     }
 
     emst::Ctx c;  // no allocation: every DevBuf below points into the scratch array
+    c.no_alloc = true;
     c.device = dev;
     c.stream = static_cast<cudaStream_t>(stream);
     c.n = n;
@@ -95,16 +109,8 @@ extern "C" emst_status emst_region_table_noalloc(const float* d_points, int64_t 
     c.nchunk = (n + emst::kLeaf - 1) / emst::kLeaf;
     int64_t L = 1;
     while (L < c.nchunk) L <<= 1;
-    const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(1024, (n + 256 * 8 - 1) / (256 * 8)));
-
-    size_t sort_bytes = 0;
-    {
-        cub::DoubleBuffer<uint64_t> keys(nullptr, nullptr);
-        cub::DoubleBuffer<uint32_t> vals(nullptr, nullptr);
-        if (cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, keys, vals, (int)n, 0, dim == 3 ? 63 : 62,
-                                            c.stream) != cudaSuccess)
-            return EMST_ECUDA;
-    }
+    const int nblk = emst::grid_reduce_blocks(n);
+    const size_t sort_bytes = emst::radix_scratch_bytes(n, emst::grid_sort_end_bit(dim));
     Carver cv{base};
     cv.take(c.ctr, 1);
     cv.take(c.part, (size_t)nblk * 6);
@@ -134,8 +140,10 @@ extern "C" emst_status emst_region_table_noalloc(const float* d_points, int64_t 
 
     // The array keeps the previous call's data: clear the counters.
     if (cudaMemsetAsync(c.ctr.p, 0, sizeof(emst::DevCounters), c.stream) != cudaSuccess) return EMST_ECUDA;
-    if (emst::grid_build(c) != cudaSuccess) return EMST_ECUDA;
-    if (emst::nns_full(c) != cudaSuccess) return EMST_ECUDA;
+    cudaError_t e = emst::grid_build(c);
+    if (e == cudaSuccess) e = emst::nns_full(c);
+    if (e == cudaErrorMemoryAllocation) return EMST_ENOMEM;  // a slice too small: nothing was allocated
+    if (e != cudaSuccess) return EMST_ECUDA;
     uint32_t err = 0;
     if (cudaMemcpyAsync(&err, &c.ctr.p->err, sizeof(err), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
         return EMST_ECUDA;

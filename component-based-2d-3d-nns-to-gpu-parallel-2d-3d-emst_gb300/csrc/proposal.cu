@@ -1,15 +1,17 @@
 // proposal.cu -- the learned proposal's data and training on the GPU:
 //
-//   * traces: while the plain method runs, sampled first-pass queries record
-//     their features; after the round, the labels -- the d2 of the shortest
-//     edge their component actually got, and whether the point's own search
-//     found that edge (it is its component's winner);
+//   * traces: while the plain method builds its round-1 neighbour lists,
+//     sampled queries record their features and, once their list is
+//     complete, the labels -- the K-th nearest distance relative to the own
+//     leaf's bound, and whether that bound could be tightened at all
+//     (written by k_knn_first, cnns_search.cuh);
 //   * training: forward and backward of the 8-32-32-2 MLP with BF16 MMA
 //     (m16n8k16, FP32 accumulate), FP32 master weights and Adam;
 //   * packing: FP32 weights into the fragment order of the fused inference.
 //
 // None of this is in the reference (its search has no learned part); the
-// proposal only orders and bounds the first search pass, see proposal.cuh.
+// proposal only sets the starting bound of the round-1 search, see
+// proposal.cuh.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -62,80 +64,6 @@ __global__ void k_pack_frag(const float* __restrict__ w, prop::Frag* __restrict_
     out->b1[lane] = w[prop::kOffB1 + lane];
     out->b2[lane] = w[prop::kOffB2 + lane];
     if (lane < 8) out->b3[lane] = lane < kOut ? w[prop::kOffB3 + lane] : 0.f;
-}
-
-__device__ __forceinline__ uint32_t sample_hash(uint32_t me, uint32_t round)
-{
-    uint32_t h = me * 0x9E3779B1u ^ (round * 0x85EBCA77u + 0x27d4eb2fu);
-    h ^= h >> 15;
-    h *= 0x2c1b3c6du;
-    h ^= h >> 12;
-    return h;
-}
-
-__global__ void k_trace_mark(uint32_t* ctl, uint64_t cap)
-{
-    ctl[1] = (uint32_t)min((uint64_t)ctl[0], cap);
-}
-
-// Sampled first-pass queries (those not already excluded by their
-// component's bound): features as the fused inference computes them.
-__global__ void k_trace_features(const uint32_t* __restrict__ list, const uint32_t* __restrict__ n_list,
-                                 const uint32_t* __restrict__ lab, const float* __restrict__ lbp,
-                                 const uint32_t* __restrict__ clb, const uint64_t* __restrict__ ckey,
-                                 const float4* __restrict__ nlo, const float4* __restrict__ nhi,
-                                 const uint32_t* __restrict__ nlab, uint32_t L, int dim, const int* __restrict__ round,
-                                 uint32_t mask, float* __restrict__ rec, uint32_t* __restrict__ ctl, uint64_t cap)
-{
-    const uint32_t total = *n_list;
-    const int r = *round;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const uint32_t me = list[i];
-        if (sample_hash(me, (uint32_t)r) & mask) continue;
-        const uint32_t labp = lab[me];
-        const float lb0 = lbp[me];
-        const uint64_t k = ckey[labp];
-        const float cb = k == kNoKey ? INFINITY : __uint_as_float((uint32_t)(k >> 32));
-        if (lb0 > cb) continue;
-        const uint32_t ol = L + (me >> 5);
-        const float4 lo = nlo[ol], hi = nhi[ol];
-        const float ex = hi.x - lo.x, ey = hi.y - lo.y, ez = dim == 3 ? hi.z - lo.z : 0.f;
-        float f[kIn];
-        prop::features(lb0, __uint_as_float(clb[labp]), cb, ex * ex + ey * ey + ez * ez, nlab[ol] == labp, r, f);
-        const uint32_t at = atomicAdd(&ctl[0], 1u);
-        if (at >= cap) continue;
-        float* o = rec + (uint64_t)at * kRec;
-        for (int j = 0; j < kIn; ++j) o[j] = f[j];
-        o[8] = 0.f;
-        o[9] = 0.f;
-        o[10] = __uint_as_float(me);  // replaced by the regression mask after the round
-        o[11] = __uint_as_float(labp);
-    }
-}
-
-// After the round's searches: each of this round's records gets its
-// component's final shortest edge (regression target, masked when there is
-// none) and whether the point's own search found exactly that edge (class
-// label: the point is its component's winner).
-__global__ void k_trace_labels(const uint64_t* __restrict__ ckey, const uint64_t* __restrict__ selkey,
-                               float* __restrict__ rec, const uint32_t* __restrict__ ctl, uint64_t cap)
-{
-    const uint64_t first = ctl[1], last = min((uint64_t)ctl[0], cap);
-    for (uint64_t i = first + blockIdx.x * blockDim.x + threadIdx.x; i < last; i += (uint64_t)gridDim.x * blockDim.x) {
-        float* o = rec + i * kRec;
-        const uint32_t labp = __float_as_uint(o[11]);
-        const uint32_t me = __float_as_uint(o[10]);
-        const uint64_t k = ckey[labp];
-        if (k == kNoKey) {
-            o[8] = 0.f;
-            o[9] = 0.f;
-            o[10] = 0.f;
-        } else {
-            o[8] = prop::lg8(__uint_as_float((uint32_t)(k >> 32)));
-            o[9] = selkey[me] == k ? 1.f : 0.f;
-            o[10] = 1.f;
-        }
-    }
 }
 
 // ----------------------------------------------------------------------------
@@ -366,25 +294,6 @@ cudaError_t proposal_pack(const float* d_weights, void* d_frag, cudaStream_t s)
 
 size_t proposal_frag_bytes() { return sizeof(prop::Frag); }
 
-cudaError_t proposal_trace_begin(Ctx& c)
-{
-    DevCounters* d = c.ctr.p;
-    k_trace_mark<<<1, 1, 0, c.stream>>>(c.trace_ctl.p, (uint64_t)c.trace_cap);
-    const uint64_t b = std::min<uint64_t>(((uint64_t)c.n + 255) / 256, (uint64_t)c.sms * 8);
-    k_trace_features<<<(unsigned)(b ? b : 1), 256, 0, c.stream>>>(
-        c.dirty.p, &d->n_dirty, c.lab.p, c.lbp.p, c.clb.p, c.ckey.p, c.nlo.p, c.nhi.p, c.nlab.p, (uint32_t)c.L, c.dim,
-        &d->round, (1u << c.trace_shift) - 1u, c.trace.p, c.trace_ctl.p, (uint64_t)c.trace_cap);
-    c.launches += 2;
-    return cudaGetLastError();
-}
-
-cudaError_t proposal_trace_end(Ctx& c)
-{
-    k_trace_labels<<<c.sms * 4, 256, 0, c.stream>>>(c.ckey.p, c.selkey.p, c.trace.p, c.trace_ctl.p,
-                                                   (uint64_t)c.trace_cap);
-    c.launches++;
-    return cudaGetLastError();
-}
 
 // Adam steps over device records; weights in/out on the host.
 static emst_status train_on_device(const float* d_rec, int64_t n, const emst_train_config* cfg, float* weights,

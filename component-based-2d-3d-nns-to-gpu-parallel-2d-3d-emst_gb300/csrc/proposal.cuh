@@ -3,19 +3,21 @@
 // shared by the fused inference (cnns_search.cuh) and the training kernels
 // (proposal.cu).
 //
-// The proposal replaces the fixed first-pass rule of the component search
-// ("search now when lbp <= 4 x the component's smallest lbp, else defer").
-// For each dirty point it predicts
-//   out0: log2(d2 of its component's shortest outgoing edge) / 8 -- the
-//         search radius: the first-pass search stops at that radius;
-//   out1: logit of "this point's search finds its component's minimum" --
-//         the visit order: points below a threshold wait for the second
-//         pass, where the component's bound, tightened by the first pass,
-//         cuts their searches short.
-// Neither output changes what is found.  A first-pass search cut short by
-// the radius leaves a certified lower bound and goes to the second pass,
-// which searches with the component's real bound, so every component's
-// minimum -- and the edge set -- is the plain method's.
+// The proposal steers the round-1 neighbour-list build (k_knn_first), the
+// dominant kernel of a solve.  There every point searches for its K nearest
+// points; the warp's walk starts from a certified bound, the K-th smallest d2
+// to the other points of the query's own leaf.  For each query the network
+// predicts
+//   out0: log2(d2 of its K-th nearest point / that certified bound) / 8, at
+//         most 0 -- the search radius: the walk starts from the predicted
+//         radius (times 2^margin), so fewer nodes and candidates fall within
+//         the bound and fewer inserts run;
+//   out1: logit of "the own leaf's bound can be tightened at all" (false when
+//         the K nearest all lie in the own leaf) -- below the threshold the
+//         query keeps the certified bound.
+// Neither output changes what is found.  A query whose predicted radius held
+// fewer than K points is searched again from the certified bound (a
+// mispredict), so every list -- and the edge set -- is the plain method's.
 #pragma once
 #include <cstdint>
 
@@ -63,24 +65,31 @@ __device__ __forceinline__ void mma16816(float (&d)[4], uint32_t a0, uint32_t a1
 
 __device__ __forceinline__ float lg8(float d2) { return log2f(fmaxf(d2, 1e-12f)) * 0.125f; }
 
-// Features of one dirty point at the start of the first pass:
-//   lb0  its lower bound of d2 to the nearest point outside its component;
-//   clb  the smallest such bound among its component's dirty points;
-//   cb   the best edge key its component holds so far (inf: none);
-//   ext2 squared diagonal of its leaf's box (local spacing);
-//   own_full its whole leaf is in its component;  round (1-based).
-__device__ __forceinline__ void features(float lb0, float clb, float cb, float ext2, bool own_full, int round,
-                                         float (&f)[kIn])
+// Features of one query of the round-1 neighbour-list build, after its warp
+// scanned the query's own leaf:
+//   t0, t2, tk  d2 of the nearest, third nearest and K-th nearest other point
+//               of the own leaf (tk: the certified bound, finite);
+//   ext2        squared diagonal of the leaf's box (the local spacing);
+//   edge2       squared distance from the point to the surface of that box
+//               (how far the leaf's points surround it);
+//   pext2       squared diagonal of the parent node's box (density around);
+//   occ         the leaf's points / 32 (cell occupancy);
+//   round       the Boruvka round, comp the component's size (1 and 1 in the
+//               round-1 build; both kept so that the inputs name the state).
+// Distances enter as log2 ratios to tk, so the features do not depend on the
+// cloud's scale.
+__device__ __forceinline__ void knn_features(float t0, float t2, float tk, float ext2, float edge2, float pext2,
+                                             float occ, int round, float comp, float (&f)[kIn])
 {
-    const bool has_cb = cb < INFINITY;
-    f[0] = lg8(lb0);
-    f[1] = lg8(clb);
-    f[2] = has_cb ? lg8(cb) : 0.f;
-    f[3] = has_cb ? 1.f : 0.f;
-    f[4] = lg8(ext2);
-    f[5] = own_full ? 1.f : 0.f;
+    const float lk = lg8(tk);
+    f[0] = lk - lg8(ext2);
+    f[1] = lg8(t0) - lk;
+    f[2] = lg8(t2) - lk;
+    f[3] = lg8(edge2) - lk;
+    f[4] = lg8(pext2) - lg8(ext2);
+    f[5] = occ;
     f[6] = 0.125f * (float)round;
-    f[7] = f[0] - f[1];
+    f[7] = lg8(comp);
 }
 
 // Warp-wide inference: lane l's features (row l of a 32 x 8 batch) in, its

@@ -45,7 +45,9 @@ class Profile(ctypes.Structure):
                 ("search_warps", ctypes.c_int64), ("search_queries", ctypes.c_int64),
                 ("first_pass_searches", ctypes.c_int64), ("first_pass_resumed", ctypes.c_int64),
                 ("first_pass_deferred", ctypes.c_int64), ("ms_knn", ctypes.c_double), ("ms_search", ctypes.c_double),
-                ("knn_launches", ctypes.c_int64), ("search_launches", ctypes.c_int64)]
+                ("knn_launches", ctypes.c_int64), ("search_launches", ctypes.c_int64),
+                ("knn_marked", ctypes.c_int64), ("knn_insert_steps", ctypes.c_int64),
+                ("knn_learned", ctypes.c_int64), ("knn_resumed", ctypes.c_int64)]
 
 
 class TrainConfig(ctypes.Structure):

@@ -119,6 +119,15 @@ typedef struct {
     double ms_search;
     int64_t knn_launches;
     int64_t search_launches;
+    /* round-1 neighbour-list build, profile contexts: candidates marked for
+     * insertion (summed over queries), insert steps (summed over warps, the
+     * busiest lane's count), queries that started from the learned radius,
+     * and of those the ones searched again from the certified bound (the
+     * proposal's mispredictions) */
+    int64_t knn_marked;
+    int64_t knn_insert_steps;
+    int64_t knn_learned;
+    int64_t knn_resumed;
 } emst_profile;
 
 /* Context lifetime.  Replaces CalculateurEMST::initialize / the static
@@ -154,7 +163,15 @@ emst_status emst_initialize(emst_ctx* ctx, const float* points, int64_t n, int d
  * the K = 2D*2^(D-1) regions (8 in 2D, 24 in 3D).  Replaces K_computeOctants
  * (EMSTOperators.h:1466-1476 -> NodeComputeOctantMD::computeOctants,
  * NodeEMST.h:1018-1296).  On rounds > 1 only points whose table holds a
- * zero-distance entry are recomputed, as the reference does (:1051-1077). */
+ * zero-distance entry are recomputed, as the reference does (:1051-1077).
+ * Each entry is the exact nearest point of its region under (d2, input id).
+ * The reference's ring search closes a face's slabs per ring and can leave a
+ * region's entry at a farther point, or empty, when the nearest one lies in
+ * a cell of a ring it already closed; a caller reading rows
+ * (emst_get_region_table) can therefore see a different table from the
+ * reference's in those rows.  The EMST edge set is the same: a point dropped
+ * that way is never a tree edge (a nearer point of another region covers
+ * it). */
 emst_status emst_compute_octants(emst_ctx* ctx);
 
 /* Per point: nearest table entry outside its component.  Replaces
@@ -253,8 +270,11 @@ emst_status emst_solve_batch(emst_ctx* ctx, const float* points, const int64_t* 
                              int32_t n_clouds, int32_t* uv, double* lengths, int64_t* n_edges);
 
 /* Device buffers in and out (points n*dim floats; uv 2*(n-1) int32;
- * length one double), no host synchronisation except the per-round
- * termination read. */
+ * length one double).  The component search runs its round loop as one CUDA
+ * graph with the termination test on the device: the host synchronises once
+ * after the loop (to read the edge count and round statistics) and once at
+ * the end.  Host-driven contexts (emst_config.host_rounds or profile) read the
+ * counters once per round. */
 emst_status emst_solve_device(emst_ctx* ctx, const float* d_points, int64_t n, int dim, int32_t* d_uv,
                               double* d_length, int64_t* n_edges);
 
@@ -287,35 +307,39 @@ emst_status emst_read_links(const char* path, int32_t* uv, int64_t cap, int64_t*
  * Learned search proposal (no counterpart in the reference; it stands beside
  * the plain search and leaves its results unchanged)
  *
- * A small network (8 inputs, two hidden layers of 32, 2 outputs; BF16
- * tensor-core inference fused into the search kernel) predicts, for each
- * point about to search, the radius its component's shortest outgoing edge
- * will have and how likely this point's own search is to find that edge.
- * The first search pass follows the prediction: points below the threshold
- * wait for the second pass (where the component's bound, tightened by the
- * first pass, cuts their searches short), the others search only up to the
- * predicted radius (times 2^margin in d2).  A search the radius cut short
- * keeps a certified lower bound and runs again in the second pass, whose
- * searches use the component's real bound, so the edge set is the plain
- * method's.
+ * It steers round 1, where every point builds its list of the
+ * EMST_ROUND1_NEIGHBOURS nearest points (the dominant step of a solve).  The
+ * plain search starts each query's walk from a certified bound: the K-th
+ * smallest squared distance to the other points of its own 32-point leaf.  A
+ * small network (8 inputs -- the own leaf's nearest, third and K-th
+ * distances, the leaf's extent and occupancy, the parent node's extent, the
+ * point's distance to its leaf's surface, the round and the component size --
+ * two hidden layers of 32, 2 outputs; BF16 tensor-core inference fused into
+ * the search kernel) predicts the ratio of the query's true K-th nearest
+ * distance to that bound, and a gate: whether the bound can be tightened at
+ * all.  Where the gate is at or above `threshold`, the walk starts from the
+ * predicted radius times 2^margin (in d2, never above the certified bound):
+ * fewer nodes and candidates fall within it.  A query whose radius held fewer
+ * than K points walks again from the certified bound, so every list -- and
+ * the edge set -- is the plain method's.
  * ------------------------------------------------------------------------- */
 
 #define EMST_ROUND1_NEIGHBOURS 6    /* list length of emst_config.round1_neighbours */
 #define EMST_PROPOSAL_WEIGHTS 1410 /* W1[8][32] b1[32] W2[32][32] b2[32] W3[32][2] b3[2], FP32 */
 #define EMST_TRACE_RECORD 12       /* floats per trace record */
 
-/* Turns the learned first pass on (weights: EMST_PROPOSAL_WEIGHTS floats)
- * or off (weights NULL).  margin: log2 factor on the predicted radius, in
- * [0, 64]; threshold: class logit at or above which a point searches in the
- * first pass.  Single-cloud solves only (batches keep the plain rule). */
+/* Turns the learned proposal on (weights: EMST_PROPOSAL_WEIGHTS floats) or
+ * off (weights NULL).  margin: log2 factor on the predicted radius (d2), in
+ * [0, 64]; threshold: gate logit at or above which a query starts from the
+ * predicted radius.  Single-cloud solves with round-1 neighbour lists only
+ * (batches keep the plain bound). */
 emst_status emst_set_proposal(emst_ctx* ctx, const float* weights, float margin, float threshold);
 
-/* Training traces: from now on, solves of this context (plain first pass)
- * record 1 in 2^sample_shift first-pass queries, up to `capacity` records in
- * total (capacity 0: off).  Record: 8 features, log2(d2 of the component's
- * shortest edge)/8, [the point's own search found that edge], 1 if the
- * component had an edge (else both targets are void), the component label
- * bits. */
+/* Training traces: from now on, solves of this context (plain search)
+ * record 1 in 2^sample_shift round-1 queries, up to `capacity` records in
+ * total (capacity 0: off).  Record: the 8 features, log2(d2 of the K-th
+ * nearest point / the own leaf's bound)/8, [that bound could be tightened],
+ * 1 if the query has K neighbours (else both targets are void), 0. */
 emst_status emst_trace_enable(emst_ctx* ctx, int64_t capacity, int sample_shift);
 emst_status emst_get_trace(emst_ctx* ctx, float* records, int64_t cap, int64_t* count);
 emst_status emst_get_trace_device(emst_ctx* ctx, const float** d_records, int64_t* count);
@@ -364,8 +388,11 @@ emst_status emst_get_search_shape(emst_ctx* ctx, int* search_shape);
  * ------------------------------------------------------------------------- */
 
 /* Largest point set emst_region_table_noalloc accepts, and the size of the
- * device array it works in (held by every GPU that loads the library until
- * the process exits). */
+ * device array it works in.  The array is a static device variable of the
+ * library: under CUDA's default lazy module loading it is placed on a device
+ * by the first emst_region_table_noalloc call there (which looks up its
+ * address) and stays until the process exits; a caller that must not see
+ * that reservation mid-run makes one call at start-up. */
 #define EMST_NOALLOC_MAX_POINTS 32768
 #define EMST_NOALLOC_SCRATCH_BYTES (12u << 20)
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own test data.
 
 Run once in a container that has the reference checkout (read-only):
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 It reads the reference's uniform point sets ({1000..6000}randomCity.2d,
 {1000,2000,10000}randomCity.3d), its golden 3000-point edge set
 (test_2D_2/outypu.links, Appendix format "NodeP = i 0 NumLinks = k j 0 ..."),
@@ -125,4 +125,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

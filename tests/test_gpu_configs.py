@@ -1,0 +1,98 @@
+"""The five benchmark configurations at their stated sizes against the oracle.
+
+Each configuration's point set comes from its seeded generator
+(emst_workloads) at full size and is solved on the GPU through the C ABI on
+the default path (the round loop as one CUDA graph).  The oracle is the CPU
+restatement: the faithful ring search of the reference (emst_oracle.c) where
+it finishes in seconds, and the kd-tree Boruvka restatement (emst_kd_oracle.c,
+the same rounds, tie-break and union rule; pinned to the faithful one in
+tests/test_oracle_golden.py) at 10^6 and 10^7 points, where the faithful
+search's overfull cells take hours.  Bit-exact: the edges added in every
+round, the per-round edge counts and every point's final root; the tree
+length to 1e-9 relative (doubles summed in another order).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import emst_workloads as W
+import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _all_host_threads():
+    O.set_threads(os.cpu_count() or 1)
+
+
+def _gpu_solve(gpu_lib, pts):
+    with gpu_lib.Emst() as e:
+        e.initialize(pts)
+        e.run()
+        uv, rounds = e.edges(with_rounds=True)
+        stats = e.round_stats()
+        labels = e.labels()
+        ne, length = e.evaluate()
+    return uv.astype(np.int64), rounds, stats, labels, ne, length
+
+
+def _check_against(pts, got, ref):
+    uv, rounds, stats, labels, ne, length = got
+    n = len(pts)
+    assert ne == n - 1
+    assert list(stats) == [int(x) for x in ref.round_edges]
+    for k in range(1, ref.rounds + 1):
+        assert np.array_equal(O.canon(uv[rounds == k]), O.canon(ref.edges[ref.edge_round == k])), "round %d" % k
+    assert np.array_equal(labels.astype(np.int64), ref.labels)
+    assert length == pytest.approx(O.length(pts, ref.edges), rel=1e-9)
+
+
+def test_config1_uniform2d_1e4(gpu_lib):
+    """10,000 uniform 2D points: the faithful restatement, the kd-tree
+    restatement and the O(N^2) Prim oracle agree with the GPU."""
+    pts = W.make("uniform2d_1e4")
+    assert pts.shape == (10000, 2)
+    got = _gpu_solve(gpu_lib, pts)
+    sp, _, _, _ = O.rescale(pts)
+    ref = O.emst(sp, "faithful")
+    _check_against(pts, got, ref)
+    kd = O.emst_kd(sp)
+    assert np.array_equal(kd.edges, ref.edges) and np.array_equal(kd.labels, ref.labels)
+    assert np.array_equal(O.canon(got[0]), O.canon(O.prim(sp)))
+    # and the one-shot host path (emst_solve)
+    with gpu_lib.Emst() as e:
+        uv, length = e.solve(pts)
+    assert np.array_equal(O.canon(uv), O.canon(ref.edges))
+    assert length == pytest.approx(got[5], rel=1e-12)
+
+
+@pytest.mark.parametrize("workload,n,dim", [("gauss3d_1e6", 1_000_000, 3), ("bezier2d_1e7", 10_000_000, 2),
+                                            ("gauss3d_1e7", 10_000_000, 3)])
+def test_full_size_config_vs_oracle(gpu_lib, workload, n, dim):
+    """gauss3d_1e6 (64 anisotropic clusters + 10% background), bezier2d_1e7
+    (256 noisy Bezier curves + 5% background) and gauss3d_1e7 (256 clusters,
+    the headline set) at full size: every round's edges, the labels and the
+    length equal the kd-tree restatement's."""
+    pts = W.make(workload)
+    assert pts.shape == (n, dim)
+    got = _gpu_solve(gpu_lib, pts)
+    sp, _, _, _ = O.rescale(pts)
+    ref = O.emst_kd(sp)
+    _check_against(pts, got, ref)
+
+
+def test_config4_all_512_clouds_vs_oracle(gpu_lib):
+    """The 512-cloud batch (sizes log-uniform in [1e3, 1e5], half 2D, half 3D,
+    uniform or 8-cluster), solved in one batched call: every cloud's edge set
+    and length equal the oracle's for that cloud alone."""
+    clouds = W.batch_clouds()
+    assert len(clouds) == 512
+    with gpu_lib.Emst() as e:
+        uvs, lens = e.solve_batch(clouds)
+    for i, pts in enumerate(clouds):
+        sp, _, _, _ = O.rescale(pts)
+        ref = O.emst_kd(sp)
+        assert np.array_equal(O.canon(uvs[i]), O.canon(ref.edges)), i
+        assert lens[i] == pytest.approx(O.length(pts, ref.edges), rel=1e-9), i

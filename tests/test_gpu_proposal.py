@@ -54,15 +54,21 @@ def _traces(gpu_lib, clouds, shift=2):
 
 
 def test_traces_are_well_formed(gpu_lib):
+    """Round-1 records: finite features, the round and component size of
+    round 1, a target radius at or below the own leaf's bound, 0/1 labels."""
     clouds = [W.gauss_mixture(50_000, 3, 64, 7), family("uniform", 30_000, 2, 8)]
     rec = _traces(gpu_lib, clouds, shift=1)
-    assert len(rec) > 10_000
-    assert np.all(np.isfinite(rec[:, :11]))
+    assert 20_000 < len(rec) < 60_000  # about half of the 80,000 queries
+    assert np.all(np.isfinite(rec))
     assert set(np.unique(rec[:, 9])) <= {0.0, 1.0} and set(np.unique(rec[:, 10])) <= {0.0, 1.0}
-    assert rec[:, 10].mean() > 0.99  # every component but the last has an edge
-    rounds = np.round(rec[:, 6] * 8).astype(int)
-    assert rounds.min() == 1 and rounds.max() >= 5
-    assert rec[rounds == 1, 9].mean() == 1.0  # in round 1 every point is its own component's winner
+    assert rec[:, 10].mean() > 0.99  # every query of a big cloud has K neighbours
+    assert np.all(rec[:, 6] == 0.125) and np.all(rec[:, 7] == 0.0)  # round 1, components of one point
+    assert np.all((rec[:, 5] > 0) & (rec[:, 5] <= 1))  # leaf occupancy
+    full = rec[:, 10] > 0
+    assert np.all(rec[full, 8] <= 0.0)  # the K-th nearest is never beyond the own leaf's bound
+    tight = rec[full, 9] > 0
+    assert np.all(rec[full][tight, 8] < 0.0) and np.all(rec[full][~tight, 8] == 0.0)
+    assert 0.2 < tight.mean() < 0.999
     # sampling: shift 2 keeps about half as many records as shift 1
     rec2 = _traces(gpu_lib, clouds, shift=2)
     assert 0.35 < len(rec2) / len(rec) < 0.65
@@ -81,35 +87,33 @@ def test_training_reduces_loss(gpu_lib):
 
 def _weight_sets(gpu_lib):
     z = np.zeros(gpu_lib.PROPOSAL_WEIGHTS, np.float32)
-    defer_all = z.copy()
-    defer_all[M.OFF_B3 + 1] = -5.0  # class logit < 0: every point waits for the second pass
+    gate_off = z.copy()
+    gate_off[M.OFF_B3 + 1] = -5.0  # gate logit < 0: every query keeps the certified bound
     tiny = z.copy()
-    tiny[M.OFF_B3] = -4.0  # radius 2^-32: every first-pass search is cut short
+    tiny[M.OFF_B3] = -4.0  # radius 2^-32 of the bound: every query is searched again
     return [("random", gpu_lib.proposal_init(3), 1.0), ("random_m0", gpu_lib.proposal_init(4), 0.0),
-            ("defer_all", defer_all, 1.0), ("tiny_radius", tiny, 0.0), ("huge_radius", gpu_lib.proposal_init(6), 40.0)]
+            ("gate_off", gate_off, 1.0), ("tiny_radius", tiny, 0.0), ("zero", z, 0.0),
+            ("huge_margin", gpu_lib.proposal_init(6), 40.0)]
 
 
 @pytest.mark.parametrize("dim", [2, 3])
 @pytest.mark.parametrize("kind", KINDS)
 @pytest.mark.parametrize("n", [2, 33, 1000, 6000])
-def test_learned_first_pass_keeps_edges_and_rounds(gpu_lib, kind, dim, n):
-    """Whatever the network predicts -- random, all deferred, a radius that cuts
-    every search short, no radius at all -- edges and per-round edge counts are
-    the plain method's."""
+def test_learned_radius_keeps_edges_and_rounds(gpu_lib, kind, dim, n):
+    """Whatever the network predicts -- random, gated off, a radius that holds
+    no neighbour at all, no tightening, a loose margin -- edges, per-round
+    edge counts and the length are the plain method's."""
     pts = family(kind, n, dim, 60 + n)
     with gpu_lib.Emst() as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
-    # wide_search -1: every list through the learned thread-per-query pass;
-    # 0: the default split, the learned pass steering the mid-length lists
-    for wide in (-1, 0):
-        for name, w, margin in _weight_sets(gpu_lib):
-            with gpu_lib.Emst(wide_search=wide) as e:
-                e.set_proposal(w, margin)
-                uv, ln = e.solve(pts)
-                assert np.array_equal(_canon(uv), _canon(ref)), (wide, name)
-                assert ln == pytest.approx(ref_len, rel=1e-12), (wide, name)
-                assert np.array_equal(e.round_stats(), ref_rounds), (wide, name)
+    for name, w, margin in _weight_sets(gpu_lib):
+        with gpu_lib.Emst() as e:
+            e.set_proposal(w, margin)
+            uv, ln = e.solve(pts)
+            assert np.array_equal(_canon(uv), _canon(ref)), name
+            assert ln == pytest.approx(ref_len, rel=1e-12), name
+            assert np.array_equal(e.round_stats(), ref_rounds), name
 
 
 def test_learned_graph_and_host_loops_agree(gpu_lib):
@@ -117,28 +121,60 @@ def test_learned_graph_and_host_loops_agree(gpu_lib):
     w = gpu_lib.proposal_init(9)
     out = []
     for host in (False, True):
-        for wide in (-1, 0):
-            with gpu_lib.Emst(host_rounds=host, wide_search=wide) as e:
-                e.set_proposal(w, 1.0)
-                out.append(_canon(e.solve(pts)[0]))
+        with gpu_lib.Emst(host_rounds=host) as e:
+            e.set_proposal(w, 1.0)
+            out.append(_canon(e.solve(pts)[0]))
     with gpu_lib.Emst() as e:
         ref = _canon(e.solve(pts)[0])
     for got in out:
         assert np.array_equal(got, ref)
 
 
-def test_first_pass_counters(gpu_lib):
+def test_learned_counters(gpu_lib):
+    """Mispredictions are counted and searched again: a radius that holds
+    nothing sends every query it steers back; a closed gate steers none."""
     pts = W.gauss_mixture(100_000, 3, 64, 22)
-    for weights in (None, gpu_lib.proposal_init(2)):
+    sets = {name: (w, m) for name, w, m in _weight_sets(gpu_lib)}
+    prof = {}
+    for name in ("plain", "tiny_radius", "gate_off", "zero"):
+        with gpu_lib.Emst(profile=True) as e:
+            if name != "plain":
+                e.set_proposal(*sets[name])
+            e.solve(pts)
+            prof[name] = e.profile()
+    assert prof["plain"]["knn_learned"] == 0 and prof["plain"]["knn_resumed"] == 0
+    assert prof["gate_off"]["knn_learned"] == 0
+    assert prof["tiny_radius"]["knn_learned"] > 0.9 * len(pts)
+    assert prof["tiny_radius"]["knn_resumed"] == prof["tiny_radius"]["knn_learned"]
+    # the zero network predicts the certified bound itself: nothing changes
+    assert prof["zero"]["knn_resumed"] == 0
+    assert prof["zero"]["knn_marked"] == prof["plain"]["knn_marked"]
+
+
+def test_trained_proposal_ablation(gpu_lib):
+    """On a fixed 10^6-point clustered set (not a training cloud): trained
+    network, untrained network and no network give the same edge set; the
+    trained network starts a large share of the queries from a radius below
+    the own leaf's bound, marks fewer candidates than the plain search, and
+    mispredicts rarely (each misprediction is searched again)."""
+    import emst_proposal as PR
+    w, info = PR.load()
+    assert w is not None, "no trained weights"
+    pts = W.gauss_mixture(1_000_000, 3, 256, 77)
+    out = {}
+    for name, weights, margin in (("plain", None, 0.0), ("untrained", gpu_lib.proposal_init(11), info["margin"]),
+                                  ("trained", w, info["margin"])):
         with gpu_lib.Emst(profile=True) as e:
             if weights is not None:
-                e.set_proposal(weights, 0.0)
-            e.solve(pts)
-            p = e.profile()
-        assert p["first_pass_searches"] > 0
-        assert 0 <= p["first_pass_resumed"] <= p["first_pass_searches"]
-        if weights is None:
-            assert p["first_pass_resumed"] == 0  # the plain first pass has no radius
+                e.set_proposal(weights, margin, info["threshold"])
+            uv, _ = e.solve(pts)
+            out[name] = (_canon(uv), e.profile())
+    for name in ("untrained", "trained"):
+        assert np.array_equal(out[name][0], out["plain"][0]), name
+    plain, trained = out["plain"][1], out["trained"][1]
+    assert trained["knn_learned"] > 0.05 * len(pts)
+    assert trained["knn_marked"] < plain["knn_marked"]
+    assert trained["knn_resumed"] < 0.05 * trained["knn_learned"]
 
 
 def test_set_proposal_rejects_bad_input(gpu_lib):

@@ -94,3 +94,36 @@ def test_region_mask_rules():
     # duplicate: every dominant axis, '+' face only (d >= 0), every slab
     assert f(0.0, 0.0) == 0b00110011
     assert f(0.0, 0.0, 0.0) == 0xF0F0F
+
+
+@pytest.mark.parametrize("key,dim", TRACED)
+def test_kd_oracle_golden_round_traces(fixtures, traces, key, dim):
+    """The kd-tree restatement reproduces the reference's recorded per-round
+    edge counts and lengths, and the 3000-point golden edges and labels."""
+    pts = fixtures[key]
+    n = len(pts)
+    trace = traces["%dd" % dim]["%drandomCity.%dd" % (n, dim)][0]
+    sp, _, _, _ = O.rescale(pts)
+    r = O.emst_kd(sp)
+    assert [int(x) for x in r.round_edges] == [row[1] for row in trace]
+    for k, row in enumerate(trace):
+        length = O.length(pts, r.edges[: r.round_edges[k]])
+        assert float("%.6g" % length) == pytest.approx(row[2], rel=1e-6)
+    if key == "pts2d_3000":
+        assert np.array_equal(O.canon(r.edges), O.canon(fixtures["outypu_edges"]))
+        assert np.array_equal(r.labels, fixtures["outypu_labels"].astype(np.int64))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("n", [2, 3, 17, 33, 1000, 5000])
+def test_kd_oracle_equals_faithful(kind, dim, n):
+    """Same edges in the same order, same rounds, same labels as the faithful
+    ring-search restatement (ties on lattices, exact duplicates, lines)."""
+    pts = family(kind, n, dim, 1000 + n)
+    sp, _, _, _ = O.rescale(pts)
+    a, b = O.emst(sp, "faithful"), O.emst_kd(sp)
+    assert np.array_equal(a.edges, b.edges)
+    assert np.array_equal(a.edge_round, b.edge_round)
+    assert list(a.round_edges) == list(b.round_edges)
+    assert np.array_equal(a.labels, b.labels)

@@ -53,14 +53,16 @@ def _regular(gpu_lib, pts):
 def test_noalloc_matches_regular_entry_point_twice(gpu_lib):
     torch = pytest.importorskip("torch")
     max_pts = _limits(gpu_lib)
-    cases = [family("cluster", 20000, 3, 31), family("dups", max_pts, 2, 32)]
+    # 3D at the limit carves the most scratch (24 regions per point)
+    cases = [family("cluster", 20000, 3, 31), family("dups", max_pts, 2, 32), family("uniform", max_pts, 3, 34)]
     for pts in cases:
         ref_ids, ref_d2 = _regular(gpu_lib, pts)
         st, ids, d2 = _noalloc(gpu_lib, torch, pts)
         assert st == 0
         assert np.array_equal(ids, ref_ids)
         assert np.array_equal(d2.view(np.uint32), ref_d2.view(np.uint32))
-    # a second call on the same data leaves device memory use unchanged
+    # a later call on the same data leaves device memory use unchanged (the
+    # first call on a device may place the library's static array there)
     free_before = torch.cuda.mem_get_info()[0]
     st, ids, d2 = _noalloc(gpu_lib, torch, cases[0])
     free_after = torch.cuda.mem_get_info()[0]
