@@ -7,9 +7,9 @@
 //      InputRW.h:545-559) and the reference's unitX in double
 //      (SolutionEMST.cu:305-341);
 //   2. the rescale p' = float(float(p - pMin) * float(unitX)) (:361-364),
-//      fused with a 48-bit Hilbert cell key per point (16 bits/axis in 3D,
-//      24 bits/axis in 2D: cells 2^-16 / 2^-24 of the extent, finer than
-//      any leaf, and a 6-pass radix sort instead of 8);
+//      fused with a 39 / 40-bit Hilbert cell key per point (13 bits/axis in
+//      3D, 20 in 2D: cells 2^-13 / 2^-20 of the extent, still finer than
+//      the leaves of the densest clusters measured, and a 5-pass radix sort);
 //   3. a radix sort of the cell keys, so points of one cell (and of
 //      neighbouring cells) are contiguous: leaves of 32 consecutive points
 //      have bounded occupancy whatever the density, unlike the reference's
@@ -30,7 +30,7 @@ namespace emst {
 
 // bits per axis of the single-cloud cell key
 template <int D>
-constexpr int kCellBits = D == 3 ? 16 : 24;
+constexpr int kCellBits = D == 3 ? 13 : 20;
 
 
 namespace {
@@ -145,7 +145,7 @@ __global__ void k_minmax_final(const float* __restrict__ part, int nblk, int64_t
     }
     np->unitx = ux;
     np->uxf = uxf;
-    const float qmax = (float)((1u << kCellBits<D>) - 1u);  // 2^16-1 / 2^24-1: exact in float
+    const float qmax = (float)((1u << kCellBits<D>) - 1u);  // 2^13-1 / 2^20-1: exact in float
     np->qscale = smax > 0.f ? qmax / smax : 0.f;
 }
 

@@ -6,7 +6,7 @@
 //                    every digit (exclusive scan, one block)
 //   k_radix_pass     per pass: a block takes the next tile of kRadixTile keys
 //                    (a ticket keeps tiles in launch order), ranks its keys
-//                    by digit in input order (warp match + per-warp counts),
+//                    by digit in input order (digit-bit ballots + per-warp counts),
 //                    publishes its per-digit counts and looks back over the
 //                    earlier tiles' counts for its output offsets (decoupled
 //                    look-back, one thread per digit), then writes keys and
@@ -123,7 +123,14 @@ __global__ void __launch_bounds__(kRadixThreads)
         const uint32_t idx = wbase + (uint32_t)i * 32u + (uint32_t)lane;
         const bool valid = idx < n;
         const uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
-        const uint32_t peers = __match_any_sync(kFullMask, valid ? d : 0x100u + (uint32_t)lane);
+        // lanes of this item holding the same digit: one ballot per digit bit
+        uint32_t peers = __ballot_sync(kFullMask, valid);
+        peers = valid ? peers : (1u << lane);
+#pragma unroll
+        for (int b = 0; b < kRadixBits; ++b) {
+            const uint32_t m = __ballot_sync(kFullMask, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? m : ~m;
+        }
         uint32_t c0 = 0;
         if (valid) c0 = s_wcnt[w][d];
         __syncwarp();
