@@ -112,15 +112,20 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         const uint64_t* __restrict__ klist, unsigned char* __restrict__ kcur,
                         const uint32_t* __restrict__ perm)
 {
-    const bool lists = klist && *round >= 2;  // round 1 builds them
+    const int r = *round;
+    const bool lists = klist && r >= 2;  // round 1 builds them
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool is_dirty = false, record = false;
+        uint64_t key = kNoKey;
+        uint32_t lp = 0;
         if (p < n) {
             const uint32_t q = selq[p];
-            const uint32_t lp = lab[p];
-            uint64_t key = kNoKey;
-            if (q != kNone && lab[q] != lp) {
+            lp = lab[p];
+            // round 2 with lists: the partner is list entry 0, the round-1
+            // edge, inside the component for certain (k_knn_first set the
+            // cursor past it)
+            if (!(lists && r == 2) && q != kNone && lab[q] != lp) {
                 key = selkey[p];
             } else {
                 uint32_t lb = __float_as_uint(lbp[p]);
@@ -166,7 +171,22 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
                 }
             }
-            if (key != kNoKey && key <= __ldcg(&ckey[lp])) {
+        }
+        // Fold the keys into the components' slots.  When every keyed lane of
+        // the warp is in one component (most warps once components are
+        // large), only the lanes holding the warp's smallest key go to the
+        // slot: the others cannot be the component's minimum.
+        const bool has = key != kNoKey;
+        const unsigned hm = __ballot_sync(kFull, has);
+        if (hm) {
+            const uint32_t l0 = __shfl_sync(kFull, lp, __ffs(hm) - 1);
+            bool go = has;
+            if (__all_sync(kFull, !has || lp == l0)) {
+                const uint32_t hi = __reduce_min_sync(kFull, has ? (uint32_t)(key >> 32) : ~0u);
+                const uint32_t lo = __reduce_min_sync(kFull, has && (uint32_t)(key >> 32) == hi ? (uint32_t)key : ~0u);
+                go = has && key == (((uint64_t)hi << 32) | lo);
+            }
+            if (go && key <= __ldcg(&ckey[lp])) {
                 const uint64_t old = atomicMin((unsigned long long*)&ckey[lp], (unsigned long long)key);
                 record = old >= key;
             }

@@ -1029,7 +1029,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 if (j == 0) p0 = pos;
                 klist[(size_t)j * n + me] = kk[j] == kNoKey ? ~0ull : ((kk[j] >> 32) << 32) | pos;
             }
-            kcur[me] = 0;
+            // entry 0 is this round's edge: inside the component from round 2 on
+            kcur[me] = kk[0] == kNoKey ? 0 : 1;
         }
         // round-1 result: entry 0 (exact: every node within the K-th
         // distance was searched)

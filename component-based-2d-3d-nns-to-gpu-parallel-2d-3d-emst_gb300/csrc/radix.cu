@@ -111,12 +111,14 @@ __global__ void __launch_bounds__(kRadixThreads)
     // warp w holds elements [w * 32 * items, (w + 1) * 32 * items), item i of
     // lane l being element i * 32 + l of that range
     uint64_t k[kRadixItems];
+    uint32_t v[kRadixItems];  // the values, loaded with the keys so that both reads overlap the ranking
     uint32_t pos[kRadixItems];
     const uint32_t wbase = base + (uint32_t)w * 32u * kRadixItems;
 #pragma unroll
     for (int i = 0; i < kRadixItems; ++i) {
         const uint32_t idx = wbase + (uint32_t)i * 32u + (uint32_t)lane;
         k[i] = idx < n ? kin[idx] : 0ull;
+        v[i] = idx < n ? vin[idx] : 0u;
     }
 #pragma unroll
     for (int i = 0; i < kRadixItems; ++i) {
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(kRadixThreads)
 #pragma unroll
     for (int i = 0; i < kRadixItems; ++i) {
         const uint32_t idx = wbase + (uint32_t)i * 32u + (uint32_t)lane;
-        if (idx < n) s_val[pos[i]] = vin[idx];
+        if (idx < n) s_val[pos[i]] = v[i];
     }
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < tile_n; j += kRadixThreads) vout[s_gbase[s_dig[j]] + j] = s_val[j];
