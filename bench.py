@@ -223,36 +223,44 @@ def edge_hash(d_uv):
     return hashlib.sha1(key.tobytes()).hexdigest()
 
 
-def learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, dim, plain_ms):
-    """Learned-vs-plain comparison on the benchmark workload: device time of the
-    same steps, edge-set identity, and the proposal's counters."""
+def learned_leg(E, args, local, stream, settings, flush, dev_pts, d_uv, d_len, n, dim):
+    """Learned-vs-plain comparison on the benchmark workload: the same steps
+    with and without the trained proposal, both on the autotuned search
+    settings with the list length the network is trained for, interleaved;
+    edge-set identity and the proposal's counters."""
     import torch
     import emst_proposal as PR
     w, info = PR.load()
     if w is None:
         return {"unavailable": "no trained weights (run emst_proposal.py)"}
-    plain_hash = edge_hash(d_uv)
     margin = float(info.get("margin", PR.DEFAULT_MARGIN))
     thr = float(info.get("threshold", PR.DEFAULT_THRESHOLD))
-    ms = []
-    with E.Emst(device=local, search_shape=shape) as lc:
-        lc.set_stream(stream.cuda_stream)
-        lc.set_proposal(w, margin, thr)
+    cfg = dict(settings)
+    cfg["round1_neighbours"] = E.ROUND1_NEIGHBOURS  # the network's list length
+    ctxs = {"plain": E.Emst(device=local, **cfg), "learned": E.Emst(device=local, **cfg)}
+    ctxs["learned"].set_proposal(w, margin, thr)
+    hashes, ms = {}, {"plain": [], "learned": []}
+    for name, c in ctxs.items():
+        c.set_stream(stream.cuda_stream)
         for _ in range(args.warmup):
-            lc.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
-        torch.cuda.synchronize()
-        for _ in range(args.steps):
+            c.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+        hashes[name] = edge_hash(d_uv)
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        for name, c in ctxs.items():
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            lc.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
+            c.solve_device(dev_pts.data_ptr(), n, dim, d_uv.data_ptr(), d_len.data_ptr())
             e1.record(stream)
             e1.synchronize()
-            ms.append(e0.elapsed_time(e1))
-    same = edge_hash(d_uv) == plain_hash
+            ms[name].append(e0.elapsed_time(e1))
+    for c in ctxs.values():
+        c.close()
+    same = hashes["learned"] == hashes["plain"]
 
     def counters(weights):
-        with E.Emst(device=local, profile=True, search_shape=shape) as pc:
+        with E.Emst(device=local, profile=True, **cfg) as pc:
             pc.set_stream(stream.cuda_stream)
             if weights is not None:
                 pc.set_proposal(weights, margin, thr)
@@ -260,7 +268,7 @@ def learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, d
             return pc.profile()
 
     pp, pl = counters(None), counters(w)
-    K = len(ms)
+    K = args.steps
 
     def per(p):
         q = max(p["search_queries"], 1)
@@ -270,14 +278,16 @@ def learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, d
                 "knn_insert_steps_per_warp": p["knn_insert_steps"] / max(n / 32, 1),
                 "knn_learned_queries": p["knn_learned"], "knn_resumed_queries": p["knn_resumed"],
                 "ms_knn": p["ms_knn"] / max(p["knn_launches"], 1)}
-    return {"value": n * K / (sum(ms) / 1e3) / 1e6, "unit": "Mpoints/s", "ms_per_step": sum(ms) / K,
-            "plain_value": n * len(plain_ms) / (sum(plain_ms) / 1e3) / 1e6, "vs_plain": sum(plain_ms) / len(plain_ms) / (sum(ms) / K),
-            "same_edge_set": same, "margin": margin, "threshold": thr,
+    mp, ml = sum(ms["plain"]) / K, sum(ms["learned"]) / K
+    return {"value": n / (ml / 1e3) / 1e6, "unit": "Mpoints/s", "ms_per_step": ml,
+            "plain_value": n / (mp / 1e3) / 1e6, "plain_ms_per_step": mp, "vs_plain": mp / ml,
+            "same_edge_set": same, "margin": margin, "threshold": thr, "settings": cfg,
             "mispredict_rate": pl["knn_resumed"] / max(pl["knn_learned"], 1),
             "plain": per(pp), "learned": per(pl),
             "weights": {k: info.get(k) for k in ("records", "clouds", "points_per_cloud", "generator", "epochs",
                                                   "loss_curve")},
-            "note": "value is the learned form; the top-level value is the plain form (the library default)"}
+            "note": "plain and learned timed interleaved on the same settings (list length of the trained "
+                    "network); the top-level value is the autotuned plain form (the library default)"}
 
 
 def run_reference(args, pts, dim):
@@ -360,16 +370,34 @@ def main():
     # per-phase CUDA events) gives the phase split and the kernel times
     ctx = E.Emst(device=local, search_mode=args.mode)
     ctx.set_stream(stream.cuda_stream)
-    # launch shape of the component search: the autotuner times each shape on
-    # this workload (before the timed region) and keeps the fastest
+    # search settings of the component search: the autotuner times the
+    # round-1 list length, the list-length thresholds of the search kernels and
+    # the thread-per-query launch shape on this workload (before the timed
+    # region) and keeps the fastest of each; the other contexts take them over
     shape, shape_ms = 0, None
+    tuning = None
     if args.mode == 0 and not args.no_autotune:
         shape, shape_ms = ctx.autotune(pts)
+        tuning = ctx.tuning()
+    settings = {} if tuning is None else {"search_shape": tuning["search_shape"], "round1_neighbours": tuning["knn_k"],
+                                          "wide_max_list": tuning["wide_max"], "coop_min_list": tuning["coop_min"]}
     _, sh_threads, sh_blocks = E.search_shapes()
     sh = shape if shape else 2  # library default: entry 2 of the table
     launch_shape = {"threads": int(sh_threads[sh - 1]), "min_blocks_per_sm": int(sh_blocks[sh - 1]),
                     "search_shape": sh, "autotuned_ms": None if shape_ms is None else [round(float(v), 3) for v in shape_ms]}
-    pctx = E.Emst(device=local, profile=True, search_mode=args.mode, search_shape=shape)
+    if tuning is not None:
+        r3 = lambda v: [round(float(x), 3) for x in v]
+        launch_shape["autotune"] = {
+            "round1_list_length": {"chosen": tuning["knn_k"], "candidates": tuning["knn_k_values"],
+                                   "ms": r3(tuning["ms_knn_k"])},
+            "coop_min_list": {"chosen": tuning["coop_min"], "candidates": tuning["coop_min_values"],
+                              "ms": r3(tuning["ms_coop_min"])},
+            "wide_max_list": {"chosen": tuning["wide_max"], "candidates": tuning["wide_max_values"],
+                              "ms": r3(tuning["ms_wide_max"])},
+            "search_shape": {"chosen": tuning["search_shape"], "ms": r3(tuning["ms_shape"])}}
+        every = [v for k in ("ms_knn_k", "ms_coop_min", "ms_wide_max", "ms_shape") for v in tuning[k] if v > 0]
+        launch_shape["autotune"]["spread"] = {"best_ms": round(min(every), 3), "worst_ms": round(max(every), 3)}
+    pctx = E.Emst(device=local, profile=True, search_mode=args.mode, **settings)
     pctx.set_stream(stream.cuda_stream)
 
     def step():
@@ -417,7 +445,7 @@ def main():
     # first search pass; its edge set must equal the plain one
     learned = None
     if args.mode == 0 and not args.no_learned and rank == 0:
-        learned = learned_leg(E, args, local, stream, shape, flush, dev_pts, d_uv, d_len, n, dim, dev_ms)
+        learned = learned_leg(E, args, local, stream, settings, flush, dev_pts, d_uv, d_len, n, dim)
 
     # profiled run(s): phase split, search counters and the dominant kernel's time
     for _ in range(args.steps):

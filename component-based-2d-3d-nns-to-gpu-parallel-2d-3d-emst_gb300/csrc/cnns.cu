@@ -110,7 +110,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag, uint32_t* __restrict__ prov,
                         uint32_t* __restrict__ n_prov, const int* __restrict__ round,
                         const uint64_t* __restrict__ klist, unsigned char* __restrict__ kcur,
-                        const uint32_t* __restrict__ perm)
+                        const uint32_t* __restrict__ perm, int knn_k)
 {
     const int r = *round;
     const bool lists = klist && r >= 2;  // round 1 builds them
@@ -138,7 +138,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     bool full = true;
                     const int j0 = kcur[p];
                     int j = j0;
-                    for (; j < kKnn; ++j) {
+                    for (; j < knn_k; ++j) {
                         const uint64_t kj = klist[(size_t)j * n + p];  // d2 bits << 32 | position
                         const uint32_t qj = (uint32_t)kj;
                         if (qj == kNone) {
@@ -159,7 +159,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     if (key == kNoKey && (j != j0 || !full)) {
                         // none outside: a full list bounds the distance from below;
                         // a short one held every other point of the cloud
-                        // (an exhausted list, j0 == kKnn, adds nothing new)
+                        // (an exhausted list, j0 == knn_k, adds nothing new)
                         lb = full ? lb : 0x7f800000u;
                         lbp[p] = __uint_as_float(lb);
                     }
@@ -636,7 +636,7 @@ cudaError_t cnns_init(Ctx& c)
     // per tile of the list compaction: counts, then list1 and list2 offsets
     if ((e = c.ensure(c.sel_tiles, 2 * ((n + kSelTile - 1) / kSelTile))) != cudaSuccess) return e;
     if (c.knn_seed && !c.cnns_warp) {
-        if ((e = c.ensure(c.klist, n * kKnn)) != cudaSuccess) return e;
+        if ((e = c.ensure(c.klist, n * c.knn_k)) != cudaSuccess) return e;
         if ((e = c.ensure(c.kcur, n)) != cudaSuccess) return e;
         if ((e = c.ensure(c.iperm, n)) != cudaSuccess) return e;
         k_inverse_perm<<<blocks_for(c.n, 256), 256, 0, c.stream>>>((uint32_t)c.n, c.perm.p, c.iperm.p);
@@ -658,7 +658,7 @@ cudaError_t cnns_select(Ctx& c)
     const bool knn = c.knn_seed && !c.cnns_warp;
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
                                                   c.clb.p, c.dflag.p, c.prov.p, &d->n_prov, &d->round,
-                                                  knn ? c.klist.p : nullptr, c.kcur.p, c.perm.p);
+                                                  knn ? c.klist.p : nullptr, c.kcur.p, c.perm.p, c.knn_k);
     c.launches++;
     // query lists in leaf order: a warp's 32 queries are neighbours, so their
     // traversals share nodes and cache lines
@@ -702,7 +702,7 @@ cudaError_t cnns_select(Ctx& c)
             a.wide_limit = 0u;
             a.coop_min = kNoCoop;
             switch (c.search_split) {
-            case 0: a.wide_limit = kWideLimit; a.coop_min = kCoopMin; break;
+            case 0: a.wide_limit = c.wide_limit; a.coop_min = c.coop_min; break;
             case 1: a.wide_limit = 0xffffffffu; break;
             case 2: a.coop_min = 0u; break;
             default: break;
@@ -714,11 +714,12 @@ cudaError_t cnns_select(Ctx& c)
                 a.n_list2 = &d->n_dirty2;
             }
             const int shape = search_shape_of(c);
+            a.knn_k = c.knn_k;
             if (knn && pass == 1) {  // round 1 only (decided on the device)
                 // the learned proposal steers the list build's starting bound
                 // (single clouds); traces record the plain build
-                const bool learned = c.learned && !pc;
-                if (c.trace_cap > 0 && !learned && !pc) {
+                const bool learned = c.learned && !pc && c.knn_k == kKnn;
+                if (c.trace_cap > 0 && !learned && !pc && c.knn_k == kKnn) {
                     a.trace = c.trace.p;
                     a.trace_ctl = c.trace_ctl.p;
                     a.trace_cap = (uint64_t)c.trace_cap;

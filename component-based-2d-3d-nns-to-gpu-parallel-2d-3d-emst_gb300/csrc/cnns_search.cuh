@@ -749,7 +749,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
 // the exact K nearest, as with one traversal per lane.  During the search a
 // list holds only its (d2 bits, input id) keys; each entry's leaf position is
 // read from iperm (input id -> position) once, when the list is written.
-template <int D, bool CL, bool LEARN>
+template <int D, bool CL, bool LEARN, int K>
 __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs a, uint64_t* __restrict__ klist,
                                                                 unsigned char* __restrict__ kcur,
                                                                 const uint32_t* __restrict__ iperm)
@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     const uint32_t n = a.n, L = a.L;
     const uint32_t* __restrict__ pcloud = a.pcloud;
     const uint32_t* __restrict__ ncloud = a.ncloud;
-    constexpr int K = kKnn, kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
+    constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
     __shared__ float4 s_pt[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
@@ -1100,7 +1100,15 @@ cudaError_t launch_knn(const CnnsArgs& a, uint64_t* klist, unsigned char* kcur, 
     const uint64_t cap = (uint64_t)sms * 4 * 4;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
-    k_knn_first<D, CL, LEARN><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm);
+    // list length: the context's choice (the learned proposal's network is trained for kKnn)
+    static_assert(kKnn == 6, "the learned proposal is trained for lists of 6");
+    switch (LEARN ? kKnn : a.knn_k) {
+    case 4: k_knn_first<D, CL, false, 4><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm); break;
+    case 5: k_knn_first<D, CL, false, 5><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm); break;
+    case 8: k_knn_first<D, CL, false, 8><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm); break;
+    case kKnn: k_knn_first<D, CL, LEARN, kKnn><<<(unsigned)b, T, 0, s>>>(a, klist, kcur, iperm); break;
+    default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

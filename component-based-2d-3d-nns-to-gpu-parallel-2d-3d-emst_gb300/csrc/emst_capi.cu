@@ -40,6 +40,7 @@ struct emst_ctx {
     cudaGraphExec_t gexec = nullptr;
     std::vector<const void*> gkey;
     int64_t body_launches = 0;
+    emst_tuning tuning = {};  // the last emst_autotune's stages
 };
 
 namespace {
@@ -350,7 +351,8 @@ emst_status build_graph(emst_ctx* x)
                                     (const void*)(intptr_t)c.trace_cap, (const void*)(intptr_t)c.trace_shift,
                                     (const void*)(intptr_t)c.n_clouds, c.pcloud.p, c.ncloud.p, c.snaps.p,
                                     (const void*)(intptr_t)c.snap_cap, c.klist.p, c.kcur.p, c.iperm.p,
-                                    (const void*)(intptr_t)(c.knn_seed ? 1 : 0)};
+                                    (const void*)(intptr_t)(c.knn_seed ? 1 : 0), (const void*)(intptr_t)c.knn_k,
+                                    (const void*)(intptr_t)c.wide_limit, (const void*)(intptr_t)c.coop_min};
     if (x->gexec && key == x->gkey) return EMST_OK;
     drop_graph(x);
     cudaGraph_t g = nullptr, body = nullptr;
@@ -455,11 +457,16 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->first_pass_factor > 0.f) c.first_pass_factor = cfg->first_pass_factor;
         c.first_pass_ordered = cfg->first_pass_ordered != 0;
         c.knn_seed = cfg->round1_neighbours >= 0;
-        if (cfg->wide_search < -1 || cfg->wide_search > 2) {
+        bool ok = cfg->round1_neighbours == 0 || cfg->round1_neighbours == -1;
+        for (int k = 0; k < emst::kNumKnnLengths; ++k) ok = ok || cfg->round1_neighbours == emst::kKnnLengths[k];
+        if (!ok || cfg->wide_search < -1 || cfg->wide_search > 2) {
             delete x;
             return EMST_EINVAL;
         }
+        if (cfg->round1_neighbours > 0) c.knn_k = cfg->round1_neighbours;
         c.search_split = cfg->wide_search;
+        if (cfg->wide_max_list > 0) c.wide_limit = cfg->wide_max_list;
+        if (cfg->coop_min_list > 0) c.coop_min = cfg->coop_min_list;
     }
     if (c.profile) {
         c.kernel_timer = kernel_timer_cb;
@@ -997,6 +1004,10 @@ emst_status emst_get_search_shape(emst_ctx* x, int* search_shape)
     return EMST_OK;
 }
 
+// Candidate values of the autotuner's stages (emst_tuning).
+constexpr uint32_t kTuneCoop[4] = {50000u, 150000u, 400000u, emst::kNoCoop};
+constexpr uint32_t kTuneWide[3] = {16384u, 65536u, 150000u};
+
 emst_status emst_autotune(emst_ctx* x, const float* points, int64_t n, int dim, int* best, double* ms, int cap)
 {
     if (!x) return EMST_EINVAL;
@@ -1012,12 +1023,11 @@ emst_status emst_autotune(emst_ctx* x, const float* points, int64_t n, int dim, 
         return set_err(x, EMST_ECUDA, "event");
     }
     emst_status st = EMST_OK;
-    double best_ms = 1e300;
-    int best_k = 0;
-    for (int k = 0; k < emst::kNumSearchShapes && st == EMST_OK; ++k) {
-        c.search_shape = k;
+    // best of two timed solves (after one warm-up solve, which also builds the
+    // graph) with the context's current settings
+    auto time_solve = [&](double& out) {
         double t = 1e300;
-        for (int rep = 0; rep < 3 && st == EMST_OK; ++rep) {  // rep 0 warms up (and builds the graph)
+        for (int rep = 0; rep < 3 && st == EMST_OK; ++rep) {
             if ((st = do_initialize(x, points, n, dim, 0)) != EMST_OK) break;
             cudaEventRecord(e0, c.stream);
             if ((st = do_run(x)) != EMST_OK) break;
@@ -1030,17 +1040,64 @@ emst_status emst_autotune(emst_ctx* x, const float* points, int64_t n, int dim, 
             cudaEventElapsedTime(&el, e0, e1);
             if (rep > 0 && el < t) t = el;
         }
-        if (ms && k < cap) ms[k] = t;
-        if (t < best_ms) {
-            best_ms = t;
-            best_k = k;
+        out = t;
+    };
+    auto argmin = [](const double* v, int m) {
+        int b = 0;
+        for (int i = 1; i < m; ++i)
+            if (v[i] < v[b]) b = i;
+        return b;
+    };
+    emst_tuning& tu = x->tuning;
+    std::memset(&tu, 0, sizeof(tu));
+    for (int k = 0; k < emst::kNumKnnLengths; ++k) tu.knn_k_values[k] = emst::kKnnLengths[k];
+    for (int k = 0; k < 4; ++k) tu.coop_min_values[k] = kTuneCoop[k];
+    for (int k = 0; k < 3; ++k) tu.wide_max_values[k] = kTuneWide[k];
+    // Coordinate descent, the stages that move a solve most first: the
+    // round-1 list length (lists on, no learned proposal -- it is trained for
+    // the default length), the list-length thresholds of the search kernels
+    // (split by length only), the thread-per-query launch shape.
+    if (c.knn_seed && !c.learned) {
+        for (int k = 0; k < emst::kNumKnnLengths && st == EMST_OK; ++k) {
+            c.knn_k = emst::kKnnLengths[k];
+            time_solve(tu.ms_knn_k[k]);
         }
+        if (st == EMST_OK) c.knn_k = emst::kKnnLengths[argmin(tu.ms_knn_k, emst::kNumKnnLengths)];
+    }
+    if (c.search_split == 0) {
+        for (int k = 0; k < 4 && st == EMST_OK; ++k) {
+            c.coop_min = kTuneCoop[k];
+            time_solve(tu.ms_coop_min[k]);
+        }
+        if (st == EMST_OK) c.coop_min = kTuneCoop[argmin(tu.ms_coop_min, 4)];
+        for (int k = 0; k < 3 && st == EMST_OK; ++k) {
+            c.wide_limit = kTuneWide[k];
+            time_solve(tu.ms_wide_max[k]);
+        }
+        if (st == EMST_OK) c.wide_limit = kTuneWide[argmin(tu.ms_wide_max, 3)];
+    }
+    for (int k = 0; k < emst::kNumSearchShapes && st == EMST_OK; ++k) {
+        c.search_shape = k;
+        time_solve(tu.ms_shape[k]);
+        if (ms && k < cap) ms[k] = tu.ms_shape[k];
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != EMST_OK) return st;
+    const int best_k = argmin(tu.ms_shape, emst::kNumSearchShapes);
     c.search_shape = best_k;
     if (best) *best = best_k + 1;
+    return EMST_OK;
+}
+
+emst_status emst_get_tuning(emst_ctx* x, emst_tuning* out)
+{
+    if (!x || !out) return EMST_EINVAL;
+    *out = x->tuning;
+    out->knn_k = x->c.knn_seed ? x->c.knn_k : 0;
+    out->coop_min = x->c.coop_min;
+    out->wide_max = x->c.wide_limit;
+    out->search_shape = emst::search_shape_of(x->c) + 1;
     return EMST_OK;
 }
 

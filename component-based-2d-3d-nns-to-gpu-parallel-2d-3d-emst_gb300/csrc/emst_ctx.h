@@ -32,6 +32,27 @@
 
 namespace emst {
 
+// Neighbours kept per point by round 1 (k_knn_first) to answer later rounds:
+// the default, and the lengths the list build is compiled for (the autotuner
+// picks one per context).
+constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
+constexpr int kNumKnnLengths = 4;
+constexpr int kKnnLengths[kNumKnnLengths] = {4, 5, 6, 8};
+constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
+constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
+constexpr int kWideWarps = 8;  // warps per block of k_cnns_w
+constexpr int kWideFan = 5;    // k_cnns_w: levels a traversal step descends (32 nodes, one per lane)
+// longest query list k_cnns_w takes (warp per query); longer lists fill the GPU
+// thread per query (k_cnns_t).  Measured at 10^7 points: 5.6k queries 0.06 vs
+// 0.41 ms, 94k queries 0.42 vs 0.37 ms
+constexpr uint32_t kWideLimit = 65536;
+// shortest query list k_cnns_c takes: rounds where enough points of a leaf
+// search that a warp's 32 queries walk mostly the same nodes.  Swept (profile
+// solves of gauss3d_1e7 / bezier2d_1e7): 150k 18.30 / 13.37 ms, 400k 18.50 /
+// 13.43, 10^6 18.57 / 13.51
+constexpr uint32_t kCoopMin = 150000;
+constexpr uint32_t kNoCoop = 0xffffffffu;
+
 // Device-side counters.  n_act / n_roots hold the CURRENT list sizes between
 // kernels; a kernel that rebuilds a list first has its input size copied to
 // the matching s_* slot (stream-ordered), then appends into the live counter.
@@ -155,14 +176,20 @@ struct Ctx {
     // (one pass); with the query lists compacted before each pass, deferring
     // measured slower on GB300 for every factor tried (1.0001 .. 16)
     float first_pass_factor = INFINITY;
-    // round 1 keeps each point's kKnn nearest (k_knn_first); later rounds take
+    // round 1 keeps each point's knn_k nearest (k_knn_first); later rounds take
     // the first entry outside the component without a search (k_reuse)
     bool knn_seed = true;
+    int knn_k = kKnn;
+    // list lengths at which the search switches kernel: up to wide_limit warp
+    // per query, above coop_min (and wide_limit) warp per 32 queries, thread
+    // per query between (search_split 0)
+    uint32_t wide_limit = kWideLimit;
+    uint32_t coop_min = kCoopMin;
     // which kernel searches a round's query list: 0 by its length (k_cnns_w
     // for short lists, k_cnns_c for long ones, k_cnns_t between), -1 k_cnns_t
     // only, 1 k_cnns_w only, 2 k_cnns_c only
     int search_split = 0;
-    // kKnn entries per point, entry-major (entry j of point p at j * n + p):
+    // knn_k entries per point, entry-major (entry j of point p at j * n + p):
     // d2 bits << 32 | leaf position, sorted by (d2, input id); ~0 = no entry
     DevBuf<uint64_t> klist;
     DevBuf<unsigned char> kcur;  // per point: leading list entries known to lie in its component
@@ -263,6 +290,8 @@ struct CnnsArgs {
     // lists longer than this (and than wide_limit) go to k_cnns_c (warp per
     // 32 queries walking together); kNoCoop: never
     uint32_t coop_min;
+    // neighbours kept per point by the round-1 list build (kKnnLengths)
+    int knn_k;
     // training traces of the round-1 list build (null: off): records of
     // prop::kRec floats, ctl[0] counts them, 1 in (mask + 1) queries sampled
     float* trace;
@@ -277,22 +306,6 @@ struct CnnsArgs {
 // 10 queries given a learned radius, 11 of those searched again.
 constexpr int kNumStats = 12;
 
-// Neighbours kept per point by round 1 (k_knn_first) to answer later rounds.
-constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
-constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
-constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
-constexpr int kWideWarps = 8;  // warps per block of k_cnns_w
-constexpr int kWideFan = 5;    // k_cnns_w: levels a traversal step descends (32 nodes, one per lane)
-// longest query list k_cnns_w takes (warp per query); longer lists fill the GPU
-// thread per query (k_cnns_t).  Measured at 10^7 points: 5.6k queries 0.06 vs
-// 0.41 ms, 94k queries 0.42 vs 0.37 ms
-constexpr uint32_t kWideLimit = 65536;
-// shortest query list k_cnns_c takes: rounds where enough points of a leaf
-// search that a warp's 32 queries walk mostly the same nodes.  Swept (profile
-// solves of gauss3d_1e7 / bezier2d_1e7): 150k 18.30 / 13.37 ms, 400k 18.50 /
-// 13.43, 10^6 18.57 / 13.51
-constexpr uint32_t kCoopMin = 150000;
-constexpr uint32_t kNoCoop = 0xffffffffu;
 
 // Launch shapes of the component search: threads per block and the minimum
 // number of resident blocks per SM the compiler must fit (which caps the

@@ -34,7 +34,16 @@ class Config(ctypes.Structure):
                 ("keep_region_table", ctypes.c_int), ("profile", ctypes.c_int), ("search_mode", ctypes.c_int),
                 ("host_rounds", ctypes.c_int), ("search_shape", ctypes.c_int),
                 ("first_pass_factor", ctypes.c_float), ("first_pass_ordered", ctypes.c_int),
-                ("round1_neighbours", ctypes.c_int), ("wide_search", ctypes.c_int)]
+                ("round1_neighbours", ctypes.c_int), ("wide_search", ctypes.c_int),
+                ("wide_max_list", ctypes.c_uint32), ("coop_min_list", ctypes.c_uint32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("knn_k", ctypes.c_int), ("coop_min", ctypes.c_uint32), ("wide_max", ctypes.c_uint32),
+                ("search_shape", ctypes.c_int), ("knn_k_values", ctypes.c_int * 4), ("ms_knn_k", ctypes.c_double * 4),
+                ("coop_min_values", ctypes.c_uint32 * 4), ("ms_coop_min", ctypes.c_double * 4),
+                ("wide_max_values", ctypes.c_uint32 * 3), ("ms_wide_max", ctypes.c_double * 3),
+                ("ms_shape", ctypes.c_double * 6)]
 
 
 class Profile(ctypes.Structure):
@@ -93,7 +102,7 @@ def lib():
             "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
             "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
             "emst_search_shape_info": [P, P, P, I], "emst_autotune": [P, P, i64, I, P, P, I],
-            "emst_get_search_shape": [P, P],
+            "emst_get_search_shape": [P, P], "emst_get_tuning": [P, P],
             "emst_set_proposal": [P, P, ctypes.c_float, ctypes.c_float], "emst_trace_enable": [P, i64, I],
             "emst_get_trace": [P, P, i64, P], "emst_get_trace_device": [P, P, P],
             "emst_proposal_init": [ctypes.c_uint64, P], "emst_proposal_train": [P, i64, I, P, P, P],
@@ -194,10 +203,11 @@ class Emst:
 
     def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False,
                  search_mode=0, host_rounds=False, search_shape=0, first_pass_factor=0.0,
-                 first_pass_ordered=False, round1_neighbours=0, wide_search=0):
+                 first_pass_ordered=False, round1_neighbours=0, wide_search=0, wide_max_list=0, coop_min_list=0):
         cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0,
                      int(search_mode), 1 if host_rounds else 0, int(search_shape), float(first_pass_factor),
-                     1 if first_pass_ordered else 0, int(round1_neighbours), int(wide_search))
+                     1 if first_pass_ordered else 0, int(round1_neighbours), int(wide_search), int(wide_max_list),
+                     int(coop_min_list))
         h = ctypes.c_void_p()
         st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:
@@ -366,6 +376,16 @@ class Emst:
         v = ctypes.c_int()
         self._chk(lib().emst_get_search_shape(self.h, ctypes.byref(v)))
         return v.value
+
+    def tuning(self):
+        """The search settings in use and the last autotune's stage tables (dict)."""
+        t = Tuning()
+        self._chk(lib().emst_get_tuning(self.h, ctypes.byref(t)))
+        return {"knn_k": t.knn_k, "coop_min": t.coop_min, "wide_max": t.wide_max, "search_shape": t.search_shape,
+                "knn_k_values": list(t.knn_k_values), "ms_knn_k": list(t.ms_knn_k),
+                "coop_min_values": list(t.coop_min_values), "ms_coop_min": list(t.ms_coop_min),
+                "wide_max_values": list(t.wide_max_values), "ms_wide_max": list(t.ms_wide_max),
+                "ms_shape": list(t.ms_shape)}
 
     # --- learned proposal ------------------------------------------------
     def set_proposal(self, weights, margin=1.0, threshold=0.0):

@@ -71,7 +71,9 @@ typedef struct {
                               EMST_ROUND1_NEIGHBOURS nearest, and later
                               rounds take the first one outside the
                               component without a search (8 bytes per entry
-                              + 1 per point); -1 = off */
+                              + 1 per point); 4, 5, 6 or 8: that many
+                              (emst_autotune picks one); -1 = off; other
+                              values: EMST_EINVAL */
     int wide_search;       /* which kernel searches a round's query list:
                               0 = default, by its length: at most 65536
                               points one warp per query (k_cnns_w), more than
@@ -81,6 +83,11 @@ typedef struct {
                               only; 1 = warp per query only; 2 = warp per 32
                               queries only.  Every choice gives the same
                               edges; other values: EMST_EINVAL */
+    uint32_t wide_max_list; /* wide_search 0: longest list searched warp
+                              per query; 0 = default (65536) */
+    uint32_t coop_min_list; /* wide_search 0: lists longer than this are
+                              searched warp per 32 queries; 0 = default
+                              (150000); 0xffffffff = never */
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel
@@ -375,13 +382,39 @@ emst_status emst_proposal_grad(const float* weights, const float* records, int64
  * resident blocks per SM it is compiled for (cap entries written). */
 emst_status emst_search_shape_info(int* count, int* threads, int* min_blocks, int cap);
 
-/* Solves `points` (host, n x dim) once per launch shape after a warm-up
- * solve, keeps the fastest shape for this context and returns its
- * emst_config.search_shape value in *best.  ms (optional, cap entries): the
- * best of two timed solves per shape.  Afterwards the context holds a
- * finished solve of `points`.  Component search mode only. */
+/* Tunes the component search on `points` (host, n x dim) by coordinate
+ * descent, each candidate timed as the best of two solves after a warm-up
+ * solve, and keeps the fastest setting of each stage for this context:
+ *   1. the round-1 list length (4, 5, 6, 8; lists on and no learned
+ *      proposal, which is trained for the default);
+ *   2. the list length above which a round is searched warp per 32 queries
+ *      (50k, 150k, 400k, never) and the one up to which warp per query
+ *      (16k, 64k, 150k) -- with wide_search 0;
+ *   3. the thread-per-query launch shape (emst_search_shape_info).
+ * *best: the chosen emst_config.search_shape value; ms (optional, cap
+ * entries): the time per shape of stage 3.  emst_get_tuning returns every
+ * stage's candidates and times.  Afterwards the context holds a finished
+ * solve of `points`.  Every setting gives the same edges.  Component search
+ * mode only. */
 emst_status emst_autotune(emst_ctx* ctx, const float* points, int64_t n, int dim, int* best, double* ms, int cap);
 emst_status emst_get_search_shape(emst_ctx* ctx, int* search_shape);
+
+typedef struct {
+    int knn_k;                   /* round-1 list length in use (0: lists off) */
+    uint32_t coop_min;           /* warp-per-32-queries threshold in use */
+    uint32_t wide_max;           /* warp-per-query threshold in use */
+    int search_shape;            /* emst_config.search_shape value in use */
+    int knn_k_values[4];         /* stage 1 candidates and their times (ms; 0: stage skipped) */
+    double ms_knn_k[4];
+    uint32_t coop_min_values[4]; /* stage 2 candidates (0xffffffff: never) and times */
+    double ms_coop_min[4];
+    uint32_t wide_max_values[3];
+    double ms_wide_max[3];
+    double ms_shape[6];          /* stage 3: per launch shape */
+} emst_tuning;
+
+/* The context's search settings and the last emst_autotune's stage tables. */
+emst_status emst_get_tuning(emst_ctx* ctx, emst_tuning* out);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free region table

@@ -244,16 +244,25 @@ def test_every_search_shape_same_edges(gpu_lib, kind, dim, n):
 
 
 def test_autotune_picks_a_shape_and_keeps_edges(gpu_lib):
-    """emst_autotune times every shape, keeps the fastest, and later solves
-    with it give the default shape's edge set."""
+    """emst_autotune times every list length, list-length threshold and
+    launch shape, keeps the fastest of each stage, and later solves with them
+    give the default settings' edge set."""
     pts = family("cluster", 30000, 3, 42)
     with gpu_lib.Emst() as e:
         ref, _ = e.solve(pts)
         assert e.search_shape() == 0
+        t0 = e.tuning()
+        assert t0["knn_k"] == gpu_lib.ROUND1_NEIGHBOURS and t0["coop_min"] == 150000 and t0["wide_max"] == 65536
         best, ms = e.autotune(pts)
         count, _, _ = gpu_lib.search_shapes()
         assert 1 <= best <= count and e.search_shape() == best
         assert np.all(np.isfinite(ms)) and np.all(ms > 0) and ms[best - 1] == ms.min()
+        t = e.tuning()
+        assert t["search_shape"] == best
+        assert t["knn_k_values"] == [4, 5, 6, 8] and all(v > 0 for v in t["ms_knn_k"])
+        assert t["knn_k"] == t["knn_k_values"][int(np.argmin(t["ms_knn_k"]))]
+        assert t["coop_min"] == t["coop_min_values"][int(np.argmin(t["ms_coop_min"]))]
+        assert t["wide_max"] == t["wide_max_values"][int(np.argmin(t["ms_wide_max"]))]
         uv, _ = e.solve(pts)
         assert np.array_equal(_canon(uv), _canon(ref))
         other = family("uniform", 5000, 2, 43)
@@ -325,7 +334,7 @@ def test_round1_neighbour_lists_keep_edges(gpu_lib, kind, dim, n):
     any edge or round, in the graph loop and the host loop."""
     pts = family(kind, n, dim, 83)
     out = []
-    for k in (-1, 0):
+    for k in (-1, 0, 4, 5, 8):  # off, default (6), every other list length
         for host in (False, True):
             with gpu_lib.Emst(round1_neighbours=k, host_rounds=host) as e:
                 uv, ln = e.solve(pts)
@@ -492,3 +501,24 @@ def test_search_split_rejects_unknown_values(gpu_lib):
     for bad in (-2, 3):
         with pytest.raises(gpu_lib.EmstError):
             gpu_lib.Emst(wide_search=bad)
+
+
+@pytest.mark.parametrize("coop,wide", [(1, 1), (50000, 16384), (0xffffffff, 150000), (10, 0xffffffff)])
+def test_list_thresholds_keep_edges(gpu_lib, coop, wide):
+    """The list-length thresholds that pick the search kernel of a round (set
+    by hand or by the autotuner) never change the edges or the rounds."""
+    pts = W.gauss_mixture(60000, 3, 16, 91)
+    with gpu_lib.Emst() as e:
+        ref, ref_len = e.solve(pts)
+        ref_rounds = e.round_stats()
+    with gpu_lib.Emst(coop_min_list=coop, wide_max_list=wide) as e:
+        uv, ln = e.solve(pts)
+        assert np.array_equal(_canon(uv), _canon(ref))
+        assert ln == pytest.approx(ref_len, rel=1e-12)
+        assert np.array_equal(e.round_stats(), ref_rounds)
+
+
+def test_bad_list_length_is_rejected(gpu_lib):
+    for k in (1, 3, 7, 9, -2):
+        with pytest.raises(gpu_lib.EmstError):
+            gpu_lib.Emst(round1_neighbours=k)
