@@ -184,7 +184,7 @@ emst_status do_octants(emst_ctx* x)
     EMST_CUDA(x, emst::round_tick(c), "round tick");
     // (component search: nothing to do here -- the node labels it prunes with
     // were written by the last flatten, or by the initialisation before round 1)
-    if (c.search_mode != 0) {
+    if (c.search_mode == 1) {
         if (c.round == 1)
             EMST_CUDA(x, emst::nns_full(c), "compute_octants");
         else
@@ -200,6 +200,8 @@ emst_status do_select(emst_ctx* x)
     Timed t(x, PH_SELECT);
     if (x->c.search_mode == 0)
         EMST_CUDA(x, emst::cnns_select(x->c), "find_next_closest");
+    else if (x->c.search_mode == 3)
+        EMST_CUDA(x, emst::dyn_select(x->c), "find_next_closest");
     else
         EMST_CUDA(x, emst::boruvka_select(x->c), "find_next_closest");
     x->stage = 3;
@@ -301,6 +303,7 @@ emst_status do_initialize(emst_ctx* x, const float* points, int64_t n, int dim, 
         EMST_CUDA(x, emst::grid_build(c), "grid build");
         EMST_CUDA(x, emst::boruvka_init(c), "init");
         if (c.search_mode == 0) EMST_CUDA(x, emst::cnns_init(c), "init");
+        if (c.search_mode == 3) EMST_CUDA(x, emst::dyn_init(c), "init");
     }
     c.round = 0;
     c.finished = false;
@@ -450,7 +453,11 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
         if (cfg->warps_per_block > 0) c.warps_per_block = cfg->warps_per_block;
         c.keep_table = cfg->keep_region_table != 0;
         c.profile = cfg->profile != 0;
-        c.search_mode = (cfg->search_mode == 1 || c.keep_table) ? 1 : 0;
+        if (cfg->search_mode < 0 || cfg->search_mode > 3) {
+            delete x;
+            return EMST_EINVAL;
+        }
+        c.search_mode = (cfg->search_mode == 1 || c.keep_table) ? 1 : (cfg->search_mode == 3 ? 3 : 0);
         c.cnns_warp = cfg->search_mode == 2;
         c.use_graph = cfg->host_rounds == 0;
         if (cfg->search_shape > 0) c.search_shape = cfg->search_shape - 1;
@@ -464,6 +471,11 @@ emst_status emst_create(const emst_config* cfg, emst_ctx** out)
             return EMST_EINVAL;
         }
         if (cfg->round1_neighbours > 0) c.knn_k = cfg->round1_neighbours;
+        if (cfg->min_find < 0 || cfg->min_find > 1 || (cfg->min_find == 1 && c.search_mode != 3)) {
+            delete x;
+            return EMST_EINVAL;
+        }
+        c.min_find = cfg->min_find;
         c.search_split = cfg->wide_search;
         if (cfg->wide_max_list > 0) c.wide_limit = cfg->wide_max_list;
         if (cfg->coop_min_list > 0) c.coop_min = cfg->coop_min_list;
@@ -514,6 +526,13 @@ emst_status emst_destroy(emst_ctx* x)
     emst::release(c.dirty2);
     emst::release(c.dflag);
     emst::release(c.sel_tiles);
+    emst::release(c.dyn_pos);
+    emst::release(c.dyn_start);
+    emst::release(c.dyn_closed);
+    emst::release(c.dyn_flag);
+    emst::release(c.dyn_dp);
+    emst::release(c.dyn_rkey);
+    emst::release(c.dyn_best);
     emst::release(c.pfrag);
     emst::release(c.trace);
     emst::release(c.trace_ctl);

@@ -145,7 +145,7 @@ struct Ctx {
     void* timer_owner = nullptr;
     int64_t knn_timed = 0, search_timed = 0;  // launches timed
     bool profile = false;
-    int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu)
+    int search_mode = 0;      // 0: component search (cnns.cu), 1: static region table (nns.cu), 3: dynamic pruning (dyn.cu)
     bool cnns_warp = false;   // component search: warp per 32 queries instead of thread per query
     bool use_graph = true;    // component search: run the round loop as one CUDA graph
     int search_shape = -1;    // component search launch shape (kSearchShapes); -1: default for the dimension
@@ -205,6 +205,17 @@ struct Ctx {
     int64_t trace_cap = 0;
     int trace_shift = 0;
     DevBuf<uint32_t> trace_ctl;
+    // dynamic-pruning search (search_mode 3, dyn.cu): leaf positions grouped
+    // by grid cell, each cell's first entry, per point and region the d2 of
+    // the nearest own-component point met, per point the closed regions
+    DevBuf<uint32_t> dyn_pos, dyn_start, dyn_closed, dyn_flag;
+    DevBuf<float> dyn_dp;
+    int dyn_dims[3] = {1, 1, 1};
+    // per-component minimum: 0 packed atomicMin on the root's slot, 1 diffusion
+    // over the forest's edges (search_mode 3; per point the key it reported
+    // this round and the diffused minimum)
+    int min_find = 0;
+    DevBuf<uint64_t> dyn_rkey, dyn_best;
     // per-round labels (EMSF snapshots): rounds kept, buffer of snap_cap * n roots
     int snap_rounds = 0;
     int64_t snap_cap = 0;
@@ -248,6 +259,9 @@ cudaError_t evaluate_length(Ctx& c, double* d_out);
 cudaError_t labels_to_input_order(Ctx& c, int32_t* d_out, const uint32_t* src = nullptr);
 cudaError_t snapshot_labels(Ctx& c);
 cudaError_t table_to_host_order(Ctx& c);
+// dyn.cu
+cudaError_t dyn_init(Ctx& c);
+cudaError_t dyn_select(Ctx& c);
 // cnns.cu
 cudaError_t cnns_init(Ctx& c);
 cudaError_t cnns_node_labels(Ctx& c);

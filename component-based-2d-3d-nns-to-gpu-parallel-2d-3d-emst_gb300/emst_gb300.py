@@ -35,7 +35,7 @@ class Config(ctypes.Structure):
                 ("host_rounds", ctypes.c_int), ("search_shape", ctypes.c_int),
                 ("first_pass_factor", ctypes.c_float), ("first_pass_ordered", ctypes.c_int),
                 ("round1_neighbours", ctypes.c_int), ("wide_search", ctypes.c_int),
-                ("wide_max_list", ctypes.c_uint32), ("coop_min_list", ctypes.c_uint32)]
+                ("wide_max_list", ctypes.c_uint32), ("coop_min_list", ctypes.c_uint32), ("min_find", ctypes.c_int)]
 
 
 class Tuning(ctypes.Structure):
@@ -203,11 +203,12 @@ class Emst:
 
     def __init__(self, device=0, max_rounds=0, keep_region_table=False, warps_per_block=0, profile=False,
                  search_mode=0, host_rounds=False, search_shape=0, first_pass_factor=0.0,
-                 first_pass_ordered=False, round1_neighbours=0, wide_search=0, wide_max_list=0, coop_min_list=0):
+                 first_pass_ordered=False, round1_neighbours=0, wide_search=0, wide_max_list=0, coop_min_list=0,
+                 min_find=0):
         cfg = Config(device, max_rounds, warps_per_block, 1 if keep_region_table else 0, 1 if profile else 0,
                      int(search_mode), 1 if host_rounds else 0, int(search_shape), float(first_pass_factor),
                      1 if first_pass_ordered else 0, int(round1_neighbours), int(wide_search), int(wide_max_list),
-                     int(coop_min_list))
+                     int(coop_min_list), int(min_find))
         h = ctypes.c_void_p()
         st = lib().emst_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != 0:

@@ -52,7 +52,14 @@ typedef struct {
     int search_mode;       /* 0: component nearest-neighbour search (default);
                               1: static-pruning region table, the reference's
                               computeOctants (implied by keep_region_table);
-                              2: component search, one warp per 32 queries */
+                              2: component search, one warp per 32 queries;
+                              3: dynamic pruning, the reference's per-round
+                              ring search over cells without a candidate
+                              table (NodeSpiralSearchMD, NodeEMST.h:67-509):
+                              per point and region the nearest own-component
+                              point bounds the search, regions close for
+                              good.  Rounds run host-driven.  Every mode
+                              gives the same edges; other values: EINVAL */
     int host_rounds;       /* != 0: drive the component search's rounds from
                               the host instead of one CUDA graph */
     int search_shape;      /* component search launch shape: 0 = default for
@@ -88,6 +95,14 @@ typedef struct {
     uint32_t coop_min_list; /* wide_search 0: lists longer than this are
                               searched warp per 32 queries; 0 = default
                               (150000); 0xffffffff = never */
+    int min_find;          /* per-component minimum outgoing edge: 0 =
+                              packed 64-bit atomicMin on the component's root
+                              slot (default); 1 = diffusion over the forest's
+                              edges until every point holds its component's
+                              minimum, the reference's tree-based alternative
+                              (K_EMST_findMinInComponentDB,
+                              EMSTOperators.h:454-915); search_mode 3 only
+                              (other combinations: EMST_EINVAL).  Same edges */
 } emst_config;
 
 /* Per-phase device times (ms, accumulated since emst_initialize) and kernel

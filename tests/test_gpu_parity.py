@@ -42,8 +42,8 @@ def _is_spanning_tree(n, edges):
     return True
 
 
-MODES = [0, 1, 2]  # 0: component search (default), 1: static region table (reference's computeOctants),
-#                    2: component search, warp per 32 queries
+MODES = [0, 1, 2, 3]  # 0: component search (default), 1: static region table (reference's computeOctants),
+#                       2: component search, warp per 32 queries, 3: dynamic pruning (ring search over cells)
 
 
 @pytest.mark.parametrize("mode", MODES)
@@ -522,3 +522,48 @@ def test_bad_list_length_is_rejected(gpu_lib):
     for k in (1, 3, 7, 9, -2):
         with pytest.raises(gpu_lib.EmstError):
             gpu_lib.Emst(round1_neighbours=k)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("n", [2, 17, 1000, 6000])
+def test_dynamic_pruning_with_diffusion_min_find(gpu_lib, kind, dim, n):
+    """search_mode 3 with the diffusion min-find (every component's minimum
+    taken over its forest instead of one atomic slot): the oracle's edges,
+    per-round counts and labels."""
+    pts = family(kind, n, dim, 2000 + n)
+    with gpu_lib.Emst(search_mode=3, min_find=1) as e:
+        e.initialize(pts)
+        e.run()
+        uv = e.edges()
+        stats = e.round_stats()
+        labels = e.labels()
+    sp, _, _, _ = O.rescale(pts)
+    r = O.emst(sp, "faithful")
+    assert np.array_equal(_canon(uv), _canon(r.edges))
+    assert list(stats) == [int(x) for x in r.round_edges]
+    assert np.array_equal(labels.astype(np.int64), r.labels)
+
+
+def test_dynamic_pruning_full_config_1e6(gpu_lib):
+    """search_mode 3 on the full gauss3d_1e6 configuration (10^6 clustered 3D
+    points, cells of any occupancy) against the default mode: same edges,
+    per-round counts and labels."""
+    pts = W.make("gauss3d_1e6")
+    out = []
+    for mode in (0, 3):
+        with gpu_lib.Emst(search_mode=mode) as e:
+            e.initialize(pts)
+            e.run()
+            out.append((_canon(e.edges()), list(e.round_stats()), e.labels()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_min_find_needs_dynamic_mode(gpu_lib):
+    for mode in (0, 1, 2):
+        with pytest.raises(gpu_lib.EmstError):
+            gpu_lib.Emst(search_mode=mode, min_find=1)
+    with pytest.raises(gpu_lib.EmstError):
+        gpu_lib.Emst(search_mode=4)
