@@ -113,7 +113,10 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         const uint32_t* __restrict__ perm, int knn_k)
 {
     const int r = *round;
-    const bool lists = klist && r >= 2;  // round 1 builds them
+    // round 1 with neighbour lists: the list build searches every point and
+    // writes every result this pass would, so the pass has nothing to do
+    if (klist && r == 1) return;
+    const bool lists = klist && r >= 2;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool is_dirty = false, record = false;
@@ -442,10 +445,12 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* s_warp
 }
 
 __global__ void __launch_bounds__(kSelThreads)
-    k_sel_count(uint32_t n, int stage, unsigned char* __restrict__ flag, const uint32_t* __restrict__ lab,
+    k_sel_count(const int* __restrict__ skip_round, uint32_t n, int stage, unsigned char* __restrict__ flag,
+                const uint32_t* __restrict__ lab,
                 const float* __restrict__ lbp, const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ clb,
                 float factor, bool two, uint32_t* __restrict__ tile_cnt, unsigned long long* __restrict__ stats)
 {
+    if (skip_round && *skip_round == 1) return;  // round 1: the list build takes every point
     __shared__ uint32_t s_warp[33];
     const uint32_t tile = blockIdx.x;
     const uint32_t p0 = tile * kSelTile + threadIdx.x * kSelItems;
@@ -492,8 +497,10 @@ __global__ void __launch_bounds__(kSelThreads)
 // Exclusive offsets of the tiles' packed counts, in place; the totals go to
 // the list counters.  One block; each thread scans a run of tiles.
 __global__ void __launch_bounds__(kScanThreads)
-    k_sel_scan(uint32_t tiles, uint32_t* __restrict__ tile_cnt, uint32_t* __restrict__ cnt1, uint32_t* __restrict__ cnt2)
+    k_sel_scan(const int* __restrict__ skip_round, uint32_t tiles, uint32_t* __restrict__ tile_cnt,
+               uint32_t* __restrict__ cnt1, uint32_t* __restrict__ cnt2)
 {
+    if (skip_round && *skip_round == 1) return;  // round 1: the list build takes every point
     __shared__ uint32_t s_warp[33];
     const uint32_t per = (tiles + kScanThreads - 1) / kScanThreads;
     const uint32_t t0 = threadIdx.x * per;
@@ -524,9 +531,11 @@ __global__ void __launch_bounds__(kScanThreads)
 }
 
 __global__ void __launch_bounds__(kSelThreads)
-    k_sel_write(uint32_t n, int stage, unsigned char* __restrict__ flag, bool two, const uint32_t* __restrict__ tile_off,
+    k_sel_write(const int* __restrict__ skip_round, uint32_t n, int stage, unsigned char* __restrict__ flag, bool two,
+                const uint32_t* __restrict__ tile_off,
                 uint32_t tiles, uint32_t* __restrict__ list1, uint32_t* __restrict__ list2)
 {
+    if (skip_round && *skip_round == 1) return;  // round 1: the list build takes every point
     __shared__ uint32_t s_warp[33];
     const uint32_t tile = blockIdx.x;
     const uint32_t p0 = tile * kSelTile + threadIdx.x * kSelItems;
@@ -563,12 +572,14 @@ __global__ void __launch_bounds__(kSelThreads)
 cudaError_t select_list(Ctx& c, int stage, float factor, uint32_t* list1, uint32_t* cnt1, uint32_t* list2,
                         uint32_t* cnt2, unsigned long long* stats)
 {
+    // with round-1 neighbour lists the list build searches every point in round 1
+    const int* skip = (c.knn_seed && !c.cnns_warp && stage == 0) ? &c.ctr.p->round : nullptr;
     const uint32_t tiles = (uint32_t)((c.n + kSelTile - 1) / kSelTile);
     const bool two = list2 != nullptr;
-    k_sel_count<<<tiles, kSelThreads, 0, c.stream>>>((uint32_t)c.n, stage, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
+    k_sel_count<<<tiles, kSelThreads, 0, c.stream>>>(skip, (uint32_t)c.n, stage, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
                                                      c.clb.p, factor, two, c.sel_tiles.p, stats);
-    k_sel_scan<<<1, kScanThreads, 0, c.stream>>>(tiles, c.sel_tiles.p, cnt1, two ? cnt2 : nullptr);
-    k_sel_write<<<tiles, kSelThreads, 0, c.stream>>>((uint32_t)c.n, stage, c.dflag.p, two, c.sel_tiles.p, tiles,
+    k_sel_scan<<<1, kScanThreads, 0, c.stream>>>(skip, tiles, c.sel_tiles.p, cnt1, two ? cnt2 : nullptr);
+    k_sel_write<<<tiles, kSelThreads, 0, c.stream>>>(skip, (uint32_t)c.n, stage, c.dflag.p, two, c.sel_tiles.p, tiles,
                                                      list1, list2);
     c.launches += 3;
     return cudaGetLastError();

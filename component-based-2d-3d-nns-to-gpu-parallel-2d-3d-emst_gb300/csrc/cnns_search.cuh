@@ -768,12 +768,14 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const pt = s_pt[w];
     uint32_t* const stack = s_stack[w];
-    const uint32_t total = *a.n_list;
+    // round 1: every point, in leaf order (the reuse pass and the list
+    // compaction leave round 1 to this kernel)
+    const uint32_t total = n;
     const uint32_t stride = gridDim.x * kKnnWarps * 32;
     for (uint32_t base0 = (blockIdx.x * kKnnWarps + w) * 32; base0 < total; base0 += stride) {
         const uint32_t qi = base0 + lane;
         const bool listed = qi < total;
-        const uint32_t me = a.list[listed ? qi : base0];
+        const uint32_t me = listed ? qi : base0;
         const float4 P = sp[me];
         const uint32_t qc = CL ? __ldg(&pcloud[me]) : 0u;
         // the list: (d2 bits << 32 | input id), sorted; positions are looked
@@ -875,14 +877,16 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 if (d2 > bd) continue;
                 const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | __float_as_uint(c.w);
                 if (key >= kk[K - 1]) continue;
-                // sorted insert, all in registers
+                // sorted insert, all in registers: the new key replaces the
+                // last entry and bubbles down (keys are distinct: ids differ)
+                kk[K - 1] = key;
 #pragma unroll
                 for (int t = K - 1; t > 0; --t) {
-                    const bool sh = key < kk[t - 1];
-                    const bool put = !sh && key < kk[t];
-                    kk[t] = sh ? kk[t - 1] : (put ? key : kk[t]);
+                    const uint64_t lo = kk[t - 1], hi = kk[t];
+                    const bool sw = hi < lo;
+                    kk[t - 1] = sw ? hi : lo;
+                    kk[t] = sw ? lo : hi;
                 }
-                if (key < kk[0]) kk[0] = key;
                 if (kk[K - 1] != kNoKey) bd = __uint_as_float((uint32_t)(kk[K - 1] >> 32));
             }
         };

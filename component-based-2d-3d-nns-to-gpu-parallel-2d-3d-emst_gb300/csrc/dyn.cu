@@ -23,7 +23,14 @@
 //     region r at squared distance dr, any candidate q of region r with
 //     d2(ps, q) > dr is strictly nearer to p than to ps: the edge (p, q) beats
 //     (ps, q), which cannot be the component's shortest outgoing edge.  A
-//     margin of 2^-10 in d2 keeps that strict after float rounding;
+//     margin of 2^-10 in d2 keeps that strict after float rounding, as long
+//     as dr is not too small against d2(ps, q): with a = |p - ps| and
+//     b = |q - ps| the exact gap d2(ps, q) - d2(p, q) is at least a (b - a),
+//     which is (a/b)(1 - a/b) b^2, while a computed d2 is within 5 * 2^-24 of
+//     itself.  So own-component points nearer than 2^-36 of the bounding
+//     box's squared diagonal are not used (a coincident point, a = 0, proves
+//     nothing: its edges tie with ps's and the ids decide); the ratio
+//     d2(ps, q) / dr then stays below 2^36, the gap above 2^-18 b^2;
 //   * per point and region, dp[r] = d2 of the nearest own-component point met
 //     in r (components only grow, so it stays valid and only shrinks), and a
 //     closed bit: once a search has covered region r out to dp[r] and met no
@@ -40,6 +47,7 @@
 // 64-bit atomicMin slot (as in the component search).  With min_find 1 the
 // diffusion alternative of the reference runs instead (k_diff_edges below).
 #include <algorithm>
+#include <cmath>
 #include <cfloat>
 #include <climits>
 
@@ -128,7 +136,8 @@ __global__ void __launch_bounds__(256) k_dyn_search(const float4* __restrict__ s
                                                     uint32_t* __restrict__ closed, uint32_t* __restrict__ selq,
                                                     uint64_t* __restrict__ selkey, uint64_t* __restrict__ ckey,
                                                     uint32_t* __restrict__ prov, uint32_t* __restrict__ n_prov,
-                                                    uint64_t* __restrict__ rkey, unsigned long long* __restrict__ stats)
+                                                    uint64_t* __restrict__ rkey, float dfloor,
+                                                    unsigned long long* __restrict__ stats)
 {
     constexpr int K = Dim<D>::K;
     constexpr uint32_t kAll = (1u << K) - 1u;
@@ -200,9 +209,11 @@ __global__ void __launch_bounds__(256) k_dyn_search(const float4* __restrict__ s
                                 const uint32_t rm = region_mask<D>(ex, ey, ez);
                                 ++st_cands;
                                 if (lab[q] == lp) {
+                                    if (d2 >= dfloor) {
 #pragma unroll
-                                    for (int r = 0; r < K; ++r)
-                                        if ((rm >> r) & 1u) d[r] = fminf(d[r], d2);
+                                        for (int r = 0; r < K; ++r)
+                                            if ((rm >> r) & 1u) d[r] = fminf(d[r], d2);
+                                    }
                                     continue;
                                 }
                                 // pruned: beyond an own-component point of one of its regions
@@ -390,14 +401,18 @@ cudaError_t dyn_select(Ctx& c)
     for (int a = 0; a < 3; ++a) g.nc[a] = c.dyn_dims[a];
     unsigned long long* st = c.profile ? c.nstats.p : nullptr;
     uint64_t* rk = c.min_find == 1 ? c.dyn_rkey.p : nullptr;
+    // the pruning floor: 2^-36 of the cells' box squared diagonal
+    double diag2 = 0.0;
+    for (int a = 0; a < c.dim; ++a) diag2 += (double)g.nc[a] * kCell * (double)g.nc[a] * kCell;
+    const float dfloor = (float)std::ldexp(diag2, -36);
     if (c.dim == 2)
         k_dyn_search<2><<<blocks_for(c.n, 256), 256, 0, c.stream>>>(
             c.sp.p, c.lab.p, (uint32_t)c.n, g, c.dyn_pos.p, c.dyn_start.p, c.dyn_dp.p, c.dyn_closed.p, c.selq.p,
-            c.selkey.p, c.ckey.p, c.prov.p, &d->n_prov, rk, st);
+            c.selkey.p, c.ckey.p, c.prov.p, &d->n_prov, rk, dfloor, st);
     else
         k_dyn_search<3><<<blocks_for(c.n, 256), 256, 0, c.stream>>>(
             c.sp.p, c.lab.p, (uint32_t)c.n, g, c.dyn_pos.p, c.dyn_start.p, c.dyn_dp.p, c.dyn_closed.p, c.selq.p,
-            c.selkey.p, c.ckey.p, c.prov.p, &d->n_prov, rk, st);
+            c.selkey.p, c.ckey.p, c.prov.p, &d->n_prov, rk, dfloor, st);
     c.launches++;
     c.nns_launches++;
     cudaError_t e = cudaGetLastError();
