@@ -730,6 +730,47 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     }
 }
 
+// Wide walk of k_knn_first: nodes one level may hold, leaves it may gather.
+constexpr int kWideFront = 128;
+constexpr int kWideLeaves = 64;
+
+// Ascending bitonic sort of 32 keys, one per lane.
+__device__ __forceinline__ uint32_t bitonic_sort32(uint32_t v, int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t o = __shfl_xor_sync(kFull, v, j);
+            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+            v = keep_min ? min(v, o) : max(v, o);
+        }
+    return v;
+}
+
+// Ascending bitonic sort of 64 keys: element e is v0 of lane e (e < 32) or
+// v1 of lane e - 32.
+__device__ __forceinline__ void bitonic_sort64(uint32_t& v0, uint32_t& v1, int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 64; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j == 32) {  // k == 64: the halves of each lane, ascending
+                const uint32_t lo = min(v0, v1), hi = max(v0, v1);
+                v0 = lo;
+                v1 = hi;
+            } else {
+                const uint32_t o0 = __shfl_xor_sync(kFull, v0, j), o1 = __shfl_xor_sync(kFull, v1, j);
+                const bool lower = (lane & j) == 0;
+                // e & k for e = lane and e = lane + 32 (they differ only for k == 32)
+                const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
+                v0 = lower == up0 ? min(v0, o0) : max(v0, o0);
+                v1 = lower == up1 ? min(v1, o1) : max(v1, o1);
+            }
+        }
+}
+
 // Round 1 with neighbour lists: each point's kKnn nearest other points (its
 // component is itself), sorted by (d2, input id) and kept for later rounds:
 // there, the first entry outside the point's component is its exact nearest
@@ -762,9 +803,15 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     const uint32_t* __restrict__ pcloud = a.pcloud;
     const uint32_t* __restrict__ ncloud = a.ncloud;
     constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
+    static_assert(kWideLeaves <= kWStack && kWideFront >= 32, "the wide walk's leaf list and frontier");
     __shared__ float4 s_pt[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
+    // the wide walk's frontier, its leaves' sort keys and boxes (lo then hi
+    // per axis); none for point batches
+    __shared__ uint32_t s_fr[kKnnWarps][CL ? 1 : kWideFront];
+    __shared__ uint32_t s_lk[kKnnWarps][CL ? 1 : kWideLeaves];
+    __shared__ float s_bx[kKnnWarps][CL ? 1 : 2 * D][kWideLeaves];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const pt = s_pt[w];
     uint32_t* const stack = s_stack[w];
@@ -876,17 +923,18 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
                 if (d2 > bd) continue;
                 const uint64_t key = ((uint64_t)__float_as_uint(d2) << 32) | __float_as_uint(c.w);
-                if (key >= kk[K - 1]) continue;
-                // sorted insert, all in registers: the new key replaces the
-                // last entry and bubbles down (keys are distinct: ids differ)
-                kk[K - 1] = key;
+                // sorted insert, all in registers and without a chain: every
+                // entry is compared with the key at once (the list is sorted,
+                // so the entries below it are a prefix; keys are distinct:
+                // ids differ), then each slot keeps its entry, takes the key
+                // or takes its predecessor
+                bool below[K];
 #pragma unroll
-                for (int t = K - 1; t > 0; --t) {
-                    const uint64_t lo = kk[t - 1], hi = kk[t];
-                    const bool sw = hi < lo;
-                    kk[t - 1] = sw ? hi : lo;
-                    kk[t] = sw ? lo : hi;
-                }
+                for (int t = 0; t < K; ++t) below[t] = kk[t] < key;
+                if (below[K - 1]) continue;
+#pragma unroll
+                for (int t = K - 1; t > 0; --t) kk[t] = below[t] ? kk[t] : (below[t - 1] ? key : kk[t - 1]);
+                kk[0] = below[0] ? kk[0] : key;
                 if (kk[K - 1] != kNoKey) bd = __uint_as_float((uint32_t)(kk[K - 1] >> 32));
             }
         };
@@ -961,9 +1009,117 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         }
         const bool learned_lane = guessed;
         bool resumed = false;
+        const uint32_t nleaves = (n + 31u) >> 5;
+        // Wide walk (single point sets): the own leaf's Hilbert neighbours
+        // first (spatially close, so every lane's bound tightens), then a
+        // gather in which each lane tests another node against the own leaf's
+        // box grown by B, the largest bound of any lane.  That box-to-box
+        // bound never exceeds a lane's node_lb (the lane's point lies in the
+        // box; rounded differences are monotone), so no node a lane still
+        // wants is dropped.  The gather starts from the siblings of the own
+        // leaf's ancestors (every other leaf lies under exactly one), all
+        // tested in one step, and descends 32 nodes a step.  The gathered
+        // leaves, with their boxes kept in shared memory, are sorted by that
+        // bound and each is scanned by the lanes still wanting it.  A frontier
+        // or leaf list that overflows (degenerate boxes, e.g. many duplicates,
+        // or a bound that reaches far) returns false before any gathered leaf
+        // is scanned, and the depth-first walk runs instead, skipping the two
+        // neighbours.
+        auto wide_walk = [&]() -> bool {
+            if (own + 1 < nleaves) {
+                const uint32_t need = __ballot_sync(kFull, wanted(node_lb(L + own + 1)));
+                if (need) scan_leaf(own + 1, need, false);
+            }
+            if (own > 0) {
+                const uint32_t need = __ballot_sync(kFull, wanted(node_lb(L + own - 1)));
+                if (need) scan_leaf(own - 1, need, false);
+            }
+            // bd is -1 on lanes without a query; a bound is never negative
+            const float B = __uint_as_float(__reduce_max_sync(kFull, __float_as_uint(fmaxf(bd, 0.f))));
+            const float4 qlo = __ldg(&nlo[L + own]), qhi = __ldg(&nhi[L + own]);
+            uint32_t* const fr = s_fr[w];
+            uint32_t* const lk = s_lk[w];
+            float(*const bx)[kWideLeaves] = s_bx[w];
+            const unsigned below = (1u << lane) - 1u;
+            const int depth = 31 - __clz(L);  // levels under the root (L is a power of two)
+            __syncwarp();
+            if (lane < depth) fr[lane] = ((L + own) >> lane) ^ 1u;
+            __syncwarp();
+            int top = depth, nl = 0;
+            while (top > 0) {
+                const int take = min(top, 32);
+                top -= take;
+                ++st_nodes;
+                uint32_t node = 0;
+                float lb = INFINITY;
+                float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+                if (lane < take) {
+                    node = fr[top + lane];
+                    lo = __ldg(&nlo[node]);
+                    hi = __ldg(&nhi[node]);
+                    const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, qhi.x), __fsub_rn(qlo.x, hi.x)), 0.f);
+                    const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, qhi.y), __fsub_rn(qlo.y, hi.y)), 0.f);
+                    const float gz =
+                        D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, qhi.z), __fsub_rn(qlo.z, hi.z)), 0.f) : 0.f;
+                    lb = d2_of<D>(gx, gy, gz);
+                }
+                const bool want = lb <= B, is_leaf = node >= L;
+                const unsigned ml = __ballot_sync(kFull, want && is_leaf);
+                const unsigned mi = __ballot_sync(kFull, want && !is_leaf);
+                const int nlf = __popc(ml), nin = __popc(mi);
+                if (nl + nlf > kWideLeaves || top + 2 * nin > kWideFront) return false;
+                __syncwarp();  // every lane has read its entry: the pushes may overwrite it
+                if (want && is_leaf) {
+                    // the sort key: the bound's bits over the entry's slot
+                    const int e = nl + __popc(ml & below);
+                    stack[e] = node - L;
+                    lk[e] = (__float_as_uint(lb) & ~(uint32_t)(kWideLeaves - 1)) | (uint32_t)e;
+                    bx[0][e] = lo.x;
+                    bx[1][e] = lo.y;
+                    bx[D][e] = hi.x;
+                    bx[D + 1][e] = hi.y;
+                    if constexpr (D == 3) {
+                        bx[2][e] = lo.z;
+                        bx[5][e] = hi.z;
+                    }
+                }
+                if (want && !is_leaf) {
+                    const int e = top + 2 * __popc(mi & below);
+                    fr[e] = 2u * node;
+                    fr[e + 1] = 2u * node + 1u;
+                }
+                nl += nlf;
+                top += 2 * nin;
+                __syncwarp();
+            }
+            // nearest first
+            uint32_t v0 = lane < nl ? lk[lane] : ~0u;
+            uint32_t v1 = lane + 32 < nl ? lk[lane + 32] : ~0u;
+            if (nl > 32) bitonic_sort64(v0, v1, lane);
+            else if (nl > 1) v0 = bitonic_sort32(v0, lane);
+            for (int i = 0; i < nl; ++i) {
+                const uint32_t e = __shfl_sync(kFull, i < 32 ? v0 : v1, i & 31) & (uint32_t)(kWideLeaves - 1);
+                const uint32_t leaf = stack[e];
+                if (leaf + 1u == own || leaf == own + 1u) continue;  // scanned above
+                ++st_nodes;
+                // the lane's node_lb of the leaf, from the kept box
+                const float gx = fmaxf(fmaxf(__fsub_rn(bx[0][e], P.x), __fsub_rn(P.x, bx[D][e])), 0.f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(bx[1][e], P.y), __fsub_rn(P.y, bx[D + 1][e])), 0.f);
+                float gz = 0.f;
+                if constexpr (D == 3) gz = fmaxf(fmaxf(__fsub_rn(bx[2][e], P.z), __fsub_rn(P.z, bx[5][e])), 0.f);
+                const uint32_t need = __ballot_sync(kFull, wanted(d2_of<D>(gx, gy, gz)));
+                if (need) scan_leaf(leaf, need, false);
+            }
+            __syncwarp();  // the list's slots are the stack of a later walk
+            return true;
+        };
         for (int attempt = 0;; ++attempt) {
             scan_leaf(own, __ballot_sync(kFull, bd >= 0.f), attempt == 0);
-            for (uint32_t v = L + own; v > 1; v >>= 1) {
+            bool done = false;
+            if constexpr (!CL) done = wide_walk();
+            // after a wide walk that gave up, the neighbours are scanned
+            const bool skip_nb = !CL;
+            for (uint32_t v = L + own; !done && v > 1; v >>= 1) {
                 const uint32_t sib = v ^ 1u;
                 ++st_nodes;
                 if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
@@ -973,9 +1129,11 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                     const uint32_t node = stack[--top];
                     ++st_nodes;
                     if (node >= L) {
+                        const uint32_t lf = node - L;
+                        if (skip_nb && (lf + 1u == own || lf == own + 1u)) continue;
                         // bounds re-checked: they may have shrunk since the push
                         const uint32_t need = __ballot_sync(kFull, wanted(node_lb(node)));
-                        if (need) scan_leaf(node - L, need, false);
+                        if (need) scan_leaf(lf, need, false);
                         continue;
                     }
                     const uint32_t c0 = 2 * node, c1 = c0 + 1;

@@ -736,6 +736,44 @@ emst_status emst_get_region_table(emst_ctx* x, int32_t* ids, float* d2, int64_t 
     return EMST_OK;
 }
 
+emst_status emst_get_neighbour_lists(emst_ctx* x, int32_t* ids, float* d2, int64_t cap, int* k)
+{
+    emst_status st = check_ready(x);
+    if (st != EMST_OK) return st;
+    Ctx& c = x->c;
+    if (c.search_mode != 0 || c.cnns_warp || !c.knn_seed || !c.klist.p)
+        return set_err(x, EMST_ESTATE, "no neighbour lists: they come from the component search with round1_neighbours >= 0");
+    if (c.round < 1) return set_err(x, EMST_ESTATE, "find_next_closest has not run");
+    const int kk = c.knn_k;
+    if (k) *k = kk;
+    const int64_t n = c.n, m = n * kk;
+    if (!ids && !d2) return EMST_OK;  // the list length only
+    if (cap < m) return set_err(x, EMST_EOVERFLOW, "list buffer too small");
+    // entries hold leaf positions; a position's input id is its point's w
+    std::vector<uint64_t> lst((size_t)m);
+    std::vector<float4> pts((size_t)n);
+    EMST_CUDA(x, cudaMemcpyAsync(lst.data(), c.klist.p, sizeof(uint64_t) * m, cudaMemcpyDeviceToHost, c.stream), "lists");
+    EMST_CUDA(x, cudaMemcpyAsync(pts.data(), c.sp.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, c.stream), "lists");
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "lists");
+    for (int64_t pos = 0; pos < n; ++pos) {
+        int32_t id;
+        std::memcpy(&id, &pts[(size_t)pos].w, sizeof(id));
+        for (int j = 0; j < kk; ++j) {
+            const uint64_t e = lst[(size_t)j * n + pos];
+            const size_t o = (size_t)id * kk + j;
+            if (e == ~0ull) {
+                if (ids) ids[o] = -1;
+                if (d2) d2[o] = INFINITY;
+                continue;
+            }
+            const uint32_t q = (uint32_t)e, bits = (uint32_t)(e >> 32);
+            if (ids) std::memcpy(&ids[o], &pts[q].w, sizeof(int32_t));
+            if (d2) std::memcpy(&d2[o], &bits, sizeof(float));
+        }
+    }
+    return EMST_OK;
+}
+
 emst_status emst_get_profile(emst_ctx* x, emst_profile* out)
 {
     emst_status st = check_ready(x);

@@ -98,6 +98,7 @@ def lib():
             "emst_test_termination": [P, P], "emst_activate": [P, P], "emst_run": [P],
             "emst_evaluate": [P, P, P], "emst_get_edges": [P, P, P, i64, P], "emst_get_labels": [P, P, i64],
             "emst_get_round_stats": [P, P, P, i64], "emst_get_region_table": [P, P, P, i64],
+            "emst_get_neighbour_lists": [P, P, P, i64, P],
             "emst_get_rescaled": [P, P, P, i64], "emst_solve": [P, P, i64, I, P, P, P],
             "emst_solve_device": [P, P, i64, I, P, P, P], "emst_get_profile": [P, P],
             "emst_region_table_noalloc": [P, i64, I, P, P, P], "emst_solve_batch": [P, P, P, P, I, P, P, P],
@@ -316,6 +317,17 @@ class Emst:
         ids = np.zeros((self.n, K), np.int32)
         d2 = np.zeros((self.n, K), np.float32)
         self._chk(lib().emst_get_region_table(self.h, _p(ids), _p(d2), self.n * K))
+        return ids, d2
+
+    def neighbour_lists(self):
+        """Round-1 neighbour lists of the last solve: ids (n, k) int32 and d2
+        (n, k) float32 in the rescaled frame, ascending by (d2, id); -1 / inf
+        past the end."""
+        k = ctypes.c_int()
+        self._chk(lib().emst_get_neighbour_lists(self.h, None, None, 0, ctypes.byref(k)))
+        ids = np.zeros((self.n, k.value), np.int32)
+        d2 = np.zeros((self.n, k.value), np.float32)
+        self._chk(lib().emst_get_neighbour_lists(self.h, _p(ids), _p(d2), ids.size, None))
         return ids, d2
 
     def profile(self):

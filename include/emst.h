@@ -252,6 +252,15 @@ emst_status emst_get_round_stats(emst_ctx* ctx, int64_t* rounds, int64_t* cum_ed
  * order face * 2^(D-1) + slab (NodeEMST.h:966-972). */
 emst_status emst_get_region_table(emst_ctx* ctx, int32_t* ids, float* d2, int64_t cap);
 
+/* The round-1 neighbour lists of a solve that built them (search_mode 0 with
+ * round1_neighbours >= 0): per point, in input order, its *k nearest other
+ * points, ascending under (squared distance in the rescaled frame, id);
+ * ids -1 and d2 +inf past the end when fewer than *k other points exist.
+ * ids and d2 hold n * (*k) entries each (either may be NULL); *k is the list
+ * length (may be NULL).  No reference counterpart: the reference keeps no
+ * per-point lists. */
+emst_status emst_get_neighbour_lists(emst_ctx* ctx, int32_t* ids, float* d2, int64_t cap, int* k);
+
 /* Phase times and launch counts since the last emst_initialize (phase times
  * need emst_config.profile != 0). */
 emst_status emst_get_profile(emst_ctx* ctx, emst_profile* out);

@@ -412,3 +412,67 @@ int64_t oracle_emst_kd(const float* sp, int64_t n, int dim, int64_t* edges_out, 
     kd_free(&t);
     return iteration;
 }
+
+/* ------------------------------------------------------------------------ */
+/* k nearest neighbours (the round-1 neighbour lists)                        */
+/* ------------------------------------------------------------------------ */
+
+/* The k nearest other points of p under (d2, id), ascending; -1 / +inf past
+ * the end when fewer than k other points exist.  A node is skipped only when
+ * its box bound exceeds the k-th entry's d2 (a point at that d2 with a lower
+ * id still enters). */
+static void kd_knn_one(const kdtree_t* t, int64_t p, int k, int64_t* ids, float* d2s)
+{
+    const float* P = t->sp + p * t->dim;
+    for (int j = 0; j < k; ++j) {
+        ids[j] = KD_NONE;
+        d2s[j] = INFINITY;
+    }
+    int64_t stack[128];
+    int top = 0;
+    stack[top++] = 0;
+    while (top > 0) {
+        int64_t node = stack[--top];
+        if (kd_lb(t, node, P) > d2s[k - 1]) continue;
+        if (t->child[node] < 0) {
+            for (int64_t j = t->lo_i[node]; j < t->hi_i[node]; ++j) {
+                int64_t q = t->idx[j];
+                if (q == p) continue;
+                float d = kd_d2(P, t->sp + q * t->dim, t->dim);
+                if (!(d < d2s[k - 1] || (d == d2s[k - 1] && (ids[k - 1] == KD_NONE || q < ids[k - 1])))) continue;
+                int s = k - 1;
+                while (s > 0 && (d < d2s[s - 1] || (d == d2s[s - 1] && q < ids[s - 1]))) {
+                    d2s[s] = d2s[s - 1];
+                    ids[s] = ids[s - 1];
+                    --s;
+                }
+                d2s[s] = d;
+                ids[s] = q;
+            }
+            continue;
+        }
+        int64_t c0 = t->child[node], c1 = c0 + 1;
+        if (kd_lb(t, c0, P) <= kd_lb(t, c1, P)) {
+            stack[top++] = c1;
+            stack[top++] = c0;
+        } else {
+            stack[top++] = c0;
+            stack[top++] = c1;
+        }
+    }
+}
+
+/* Every point's k nearest other points: ids_out / d2_out hold n rows of k. */
+int oracle_knn_kd(const float* sp, int64_t n, int dim, int k, int64_t* ids_out, float* d2_out)
+{
+    if (n < 1 || k < 1 || (dim != 2 && dim != 3)) return -1;
+    kdtree_t t;
+    if (kd_build(&t, sp, n, dim) != 0) {
+        kd_free(&t);
+        return -2;
+    }
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < n; ++i) kd_knn_one(&t, i, k, ids_out + i * k, d2_out + i * k);
+    kd_free(&t);
+    return 0;
+}

@@ -55,6 +55,8 @@ def lib():
         L.oracle_kruskal_table.restype = i64
         L.oracle_emst_kd.argtypes = [P, i64, ctypes.c_int, P, P, P, P]
         L.oracle_emst_kd.restype = i64
+        L.oracle_knn_kd.argtypes = [P, i64, ctypes.c_int, ctypes.c_int, P, P]
+        L.oracle_knn_kd.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -142,6 +144,20 @@ def emst_kd(scaled):
         raise ValueError("oracle_emst_kd failed (%d)" % r)
     ne = int(rounds_e[r - 1]) if r > 0 else 0
     return EmstResult(edges[:ne].copy(), eround[:ne].copy(), rounds_e[:r].copy(), labels, None, None, int(r), 0)
+
+
+def knn(scaled, k):
+    """Every point's k nearest other points under (d2, id) by kd-tree
+    (emst_kd_oracle.c): ids (n, k) int64 and d2 (n, k) float32, ascending;
+    -1 / inf past the end when fewer than k other points exist."""
+    sp = np.ascontiguousarray(scaled, dtype=np.float32)
+    n, dim = sp.shape
+    ids = np.zeros((n, k), np.int64)
+    d2 = np.zeros((n, k), np.float32)
+    rc = lib().oracle_knn_kd(_ptr(sp), n, dim, int(k), _ptr(ids), _ptr(d2))
+    if rc != 0:
+        raise ValueError("oracle_knn_kd failed (%d)" % rc)
+    return ids, d2
 
 
 def region_table(scaled, mode="exact", level_radius=1):

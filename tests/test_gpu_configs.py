@@ -96,3 +96,17 @@ def test_config4_all_512_clouds_vs_oracle(gpu_lib):
         ref = O.emst_kd(sp)
         assert np.array_equal(O.canon(uvs[i]), O.canon(ref.edges)), i
         assert lens[i] == pytest.approx(O.length(pts, ref.edges), rel=1e-9), i
+
+
+@pytest.mark.parametrize("workload", ["gauss3d_1e6", "bezier2d_1e7", "gauss3d_1e7"])
+def test_full_size_neighbour_lists_vs_oracle(gpu_lib, workload):
+    """The round-1 neighbour lists (6 per point) of the full configurations:
+    every id and squared distance equals the kd-tree oracle's k nearest."""
+    pts = W.make(workload)
+    with gpu_lib.Emst() as e:
+        e.solve(pts)
+        ids, d2 = e.neighbour_lists()
+    sp, _, _, _ = O.rescale(pts)
+    rid, rd2 = O.knn(sp, ids.shape[1])
+    bad = np.flatnonzero((ids.astype(np.int64) != rid).any(axis=1) | (d2 != rd2).any(axis=1))
+    assert len(bad) == 0, (len(bad), bad[:5])

@@ -327,6 +327,36 @@ def test_first_pass_rules_keep_edges(gpu_lib, kw, kind, dim, wide):
         assert np.array_equal(e.round_stats(), ref_rounds)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("n", [2, 7, 33, 20000])
+def test_round1_neighbour_lists_exact(gpu_lib, kind, dim, n):
+    """Every round-1 list is the exact k nearest other points under (d2, id),
+    for every list length: ids and squared distances bit-exact against the
+    kd-tree oracle (sets of fewer than k + 1 points end in -1 / inf), in the
+    graph loop and the host loop."""
+    pts = family(kind, n, dim, 97 + n)
+    sp, _, _, _ = O.rescale(pts)
+    for k in (4, 5, 6, 8):
+        rid, rd2 = O.knn(sp, k)
+        for host in (False, True):
+            with gpu_lib.Emst(round1_neighbours=0 if k == 6 else k, host_rounds=host) as e:
+                e.solve(pts)
+                ids, d2 = e.neighbour_lists()
+            assert ids.shape == (n, k)
+            assert np.array_equal(ids.astype(np.int64), rid), (k, host)
+            assert np.array_equal(d2, rd2), (k, host)
+
+
+def test_neighbour_lists_need_the_list_search(gpu_lib):
+    pts = family("uniform", 500, 2, 5)
+    for kw in ({"round1_neighbours": -1}, {"search_mode": 1}, {"search_mode": 2}, {"search_mode": 3}):
+        with gpu_lib.Emst(**kw) as e:
+            e.solve(pts)
+            with pytest.raises(gpu_lib.EmstError):
+                e.neighbour_lists()
+
+
 @pytest.mark.parametrize("kind,dim,n", [("cluster", 3, 30000), ("uniform", 2, 30000), ("dups", 3, 8000),
                                         ("lattice", 2, 5000), ("line", 3, 3000), ("dups", 2, 9)])
 def test_round1_neighbour_lists_keep_edges(gpu_lib, kind, dim, n):

@@ -6,6 +6,7 @@ import pytest
 
 import emst_workloads as W
 import mlp_oracle as M
+import pyoracle as O
 from families import KINDS, family
 
 pytestmark = pytest.mark.gpu
@@ -102,11 +103,13 @@ def _weight_sets(gpu_lib):
 def test_learned_radius_keeps_edges_and_rounds(gpu_lib, kind, dim, n):
     """Whatever the network predicts -- random, gated off, a radius that holds
     no neighbour at all, no tightening, a loose margin -- edges, per-round
-    edge counts and the length are the plain method's."""
+    edge counts and the length are the plain method's, and every round-1
+    list is the exact 6 nearest (the kd-tree oracle's ids and d2)."""
     pts = family(kind, n, dim, 60 + n)
     with gpu_lib.Emst() as e:
         ref, ref_len = e.solve(pts)
         ref_rounds = e.round_stats()
+    rid, rd2 = O.knn(O.rescale(pts)[0], 6)
     for name, w, margin in _weight_sets(gpu_lib):
         with gpu_lib.Emst() as e:
             e.set_proposal(w, margin)
@@ -114,6 +117,9 @@ def test_learned_radius_keeps_edges_and_rounds(gpu_lib, kind, dim, n):
             assert np.array_equal(_canon(uv), _canon(ref)), name
             assert ln == pytest.approx(ref_len, rel=1e-12), name
             assert np.array_equal(e.round_stats(), ref_rounds), name
+            # and the lists themselves stay the exact 6 nearest
+            ids, d2 = e.neighbour_lists()
+            assert np.array_equal(ids.astype(np.int64), rid) and np.array_equal(d2, rd2), name
 
 
 def test_learned_graph_and_host_loops_agree(gpu_lib):
