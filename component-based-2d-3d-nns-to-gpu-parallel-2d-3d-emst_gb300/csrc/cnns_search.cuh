@@ -737,9 +737,9 @@ constexpr int kWideLeaves = 64;
 // Ascending bitonic sort of 32 keys, one per lane.
 __device__ __forceinline__ uint32_t bitonic_sort32(uint32_t v, int lane)
 {
-#pragma unroll
+#pragma unroll 1
     for (int k = 2; k <= 32; k <<= 1)
-#pragma unroll
+#pragma unroll 1
         for (int j = k >> 1; j > 0; j >>= 1) {
             const uint32_t o = __shfl_xor_sync(kFull, v, j);
             const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
@@ -752,9 +752,9 @@ __device__ __forceinline__ uint32_t bitonic_sort32(uint32_t v, int lane)
 // v1 of lane e - 32.
 __device__ __forceinline__ void bitonic_sort64(uint32_t& v0, uint32_t& v1, int lane)
 {
-#pragma unroll
+#pragma unroll 1
     for (int k = 2; k <= 64; k <<= 1)
-#pragma unroll
+#pragma unroll 1
         for (int j = k >> 1; j > 0; j >>= 1) {
             if (j == 32) {  // k == 64: the halves of each lane, ascending
                 const uint32_t lo = min(v0, v1), hi = max(v0, v1);
@@ -882,7 +882,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             if (!staged) stage_leaf(b, m);
             uint32_t mask = 0;
             if (__popc(need) > kKnnDense) {
-#pragma unroll
+#pragma unroll 8
                 for (int j = 0; j < 32; ++j) {
                     const float4 c = pt[j];
                     const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
@@ -960,7 +960,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             float t[K];
 #pragma unroll
             for (int i = 0; i < K; ++i) t[i] = INFINITY;
-#pragma unroll
+#pragma unroll 4
             for (int j = 0; j < 32; ++j) {
                 const float4 c = pt[j];
                 float d = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
@@ -1010,30 +1010,21 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         const bool learned_lane = guessed;
         bool resumed = false;
         const uint32_t nleaves = (n + 31u) >> 5;
-        // Wide walk (single point sets): the own leaf's Hilbert neighbours
-        // first (spatially close, so every lane's bound tightens), then a
-        // gather in which each lane tests another node against the own leaf's
-        // box grown by B, the largest bound of any lane.  That box-to-box
-        // bound never exceeds a lane's node_lb (the lane's point lies in the
-        // box; rounded differences are monotone), so no node a lane still
-        // wants is dropped.  The gather starts from the siblings of the own
-        // leaf's ancestors (every other leaf lies under exactly one), all
-        // tested in one step, and descends 32 nodes a step.  The gathered
-        // leaves, with their boxes kept in shared memory, are sorted by that
-        // bound and each is scanned by the lanes still wanting it.  A frontier
-        // or leaf list that overflows (degenerate boxes, e.g. many duplicates,
-        // or a bound that reaches far) returns false before any gathered leaf
-        // is scanned, and the depth-first walk runs instead, skipping the two
-        // neighbours.
-        auto wide_walk = [&]() -> bool {
-            if (own + 1 < nleaves) {
-                const uint32_t need = __ballot_sync(kFull, wanted(node_lb(L + own + 1)));
-                if (need) scan_leaf(own + 1, need, false);
-            }
-            if (own > 0) {
-                const uint32_t need = __ballot_sync(kFull, wanted(node_lb(L + own - 1)));
-                if (need) scan_leaf(own - 1, need, false);
-            }
+        // Gather (single point sets), run once the own leaf and its Hilbert
+        // neighbours are scanned (spatially close, they tighten every lane's
+        // bound): each lane tests another node against the own leaf's box
+        // grown by B, the largest bound of any lane.  That box-to-box bound
+        // never exceeds a lane's node_lb (the lane's point lies in the box;
+        // rounded differences are monotone), so no node a lane still wants is
+        // dropped.  It starts from the siblings of the own leaf's ancestors
+        // (every other leaf lies under exactly one), all tested in one step,
+        // and descends 32 nodes a step.  The gathered leaves keep their boxes
+        // in shared memory and their ids in the stack's slots; their sort keys
+        // (the bound's bits over the slot) come back sorted in v0 / v1, nearest
+        // first.  Returns the number of leaves, or -1 when the frontier or the
+        // leaf list overflows (degenerate boxes, e.g. many duplicates, or a
+        // bound that reaches far): the depth-first walk then runs instead.
+        auto gather = [&](uint32_t& v0, uint32_t& v1) -> int {
             // bd is -1 on lanes without a query; a bound is never negative
             const float B = __uint_as_float(__reduce_max_sync(kFull, __float_as_uint(fmaxf(bd, 0.f))));
             const float4 qlo = __ldg(&nlo[L + own]), qhi = __ldg(&nhi[L + own]);
@@ -1067,10 +1058,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 const unsigned ml = __ballot_sync(kFull, want && is_leaf);
                 const unsigned mi = __ballot_sync(kFull, want && !is_leaf);
                 const int nlf = __popc(ml), nin = __popc(mi);
-                if (nl + nlf > kWideLeaves || top + 2 * nin > kWideFront) return false;
+                if (nl + nlf > kWideLeaves || top + 2 * nin > kWideFront) return -1;
                 __syncwarp();  // every lane has read its entry: the pushes may overwrite it
                 if (want && is_leaf) {
-                    // the sort key: the bound's bits over the entry's slot
                     const int e = nl + __popc(ml & below);
                     stack[e] = node - L;
                     lk[e] = (__float_as_uint(lb) & ~(uint32_t)(kWideLeaves - 1)) | (uint32_t)e;
@@ -1092,63 +1082,116 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 top += 2 * nin;
                 __syncwarp();
             }
-            // nearest first
-            uint32_t v0 = lane < nl ? lk[lane] : ~0u;
-            uint32_t v1 = lane + 32 < nl ? lk[lane + 32] : ~0u;
+            v0 = lane < nl ? lk[lane] : ~0u;
+            v1 = lane + 32 < nl ? lk[lane + 32] : ~0u;
             if (nl > 32) bitonic_sort64(v0, v1, lane);
             else if (nl > 1) v0 = bitonic_sort32(v0, lane);
-            for (int i = 0; i < nl; ++i) {
-                const uint32_t e = __shfl_sync(kFull, i < 32 ? v0 : v1, i & 31) & (uint32_t)(kWideLeaves - 1);
-                const uint32_t leaf = stack[e];
-                if (leaf + 1u == own || leaf == own + 1u) continue;  // scanned above
-                ++st_nodes;
-                // the lane's node_lb of the leaf, from the kept box
-                const float gx = fmaxf(fmaxf(__fsub_rn(bx[0][e], P.x), __fsub_rn(P.x, bx[D][e])), 0.f);
-                const float gy = fmaxf(fmaxf(__fsub_rn(bx[1][e], P.y), __fsub_rn(P.y, bx[D + 1][e])), 0.f);
-                float gz = 0.f;
-                if constexpr (D == 3) gz = fmaxf(fmaxf(__fsub_rn(bx[2][e], P.z), __fsub_rn(P.z, bx[5][e])), 0.f);
-                const uint32_t need = __ballot_sync(kFull, wanted(d2_of<D>(gx, gy, gz)));
-                if (need) scan_leaf(leaf, need, false);
-            }
-            __syncwarp();  // the list's slots are the stack of a later walk
-            return true;
+            return nl;
         };
         for (int attempt = 0;; ++attempt) {
-            scan_leaf(own, __ballot_sync(kFull, bd >= 0.f), attempt == 0);
-            bool done = false;
-            if constexpr (!CL) done = wide_walk();
-            // after a wide walk that gave up, the neighbours are scanned
-            const bool skip_nb = !CL;
-            for (uint32_t v = L + own; !done && v > 1; v >>= 1) {
-                const uint32_t sib = v ^ 1u;
-                ++st_nodes;
-                if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
-                int top = 0;
-                stack[top++] = sib;
-                while (top > 0) {
-                    const uint32_t node = stack[--top];
-                    ++st_nodes;
-                    if (node >= L) {
-                        const uint32_t lf = node - L;
-                        if (skip_nb && (lf + 1u == own || lf == own + 1u)) continue;
-                        // bounds re-checked: they may have shrunk since the push
-                        const uint32_t need = __ballot_sync(kFull, wanted(node_lb(node)));
-                        if (need) scan_leaf(lf, need, false);
+            // The leaves to scan come from a warp-uniform state machine, so
+            // that every one goes through the single scan below (one copy of
+            // its code): the own leaf; for single point sets its Hilbert
+            // neighbours and then the gathered leaves, nearest first; the
+            // depth-first walk (the own leaf's ancestors' sibling subtrees, a
+            // node entered when any lane's lower bound reaches it) when the
+            // gather gives up, and for point batches.
+            enum { kOwn, kNext, kPrev, kGathered, kWalk, kDone };
+            int phase = kOwn;
+            int li = 0, nl = -2;        // gathered leaves: next index, count (-2: not gathered yet)
+            uint32_t v0 = ~0u, v1 = ~0u;  // their sorted keys
+            uint32_t dv = L + own;      // the walk: the ancestor whose sibling comes next
+            int top = 0;                // the walk's stack depth
+            while (phase != kDone) {
+                uint32_t leaf = 0, need = 0;
+                bool staged = false;
+                if (phase == kOwn) {
+                    leaf = own;
+                    need = __ballot_sync(kFull, bd >= 0.f);
+                    staged = attempt == 0;  // the bound above left it in shared memory
+                    phase = CL ? kWalk : kNext;
+                } else if (phase == kNext) {
+                    phase = kPrev;
+                    if (own + 1 < nleaves) {
+                        leaf = own + 1;
+                        need = __ballot_sync(kFull, wanted(node_lb(L + leaf)));
+                    }
+                } else if (phase == kPrev) {
+                    phase = kGathered;
+                    if (own > 0) {
+                        leaf = own - 1;
+                        need = __ballot_sync(kFull, wanted(node_lb(L + leaf)));
+                    }
+                } else if (phase == kGathered) {
+                    if (nl == -2) {
+                        nl = gather(v0, v1);
+                        if (nl < 0) {
+                            phase = kWalk;
+                            continue;
+                        }
+                    }
+                    if (li >= nl) {
+                        phase = kDone;
                         continue;
                     }
-                    const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                    const float l0 = node_lb(c0), l1 = node_lb(c1);
-                    const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
-                    // the child nearer to the warp's nearest lane is searched next
-                    const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
-                    const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
-                    const bool near0 = m0 <= m1;
-                    const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
-                    __syncwarp();  // every lane has read the popped entry
-                    if (wf) stack[top++] = near0 ? c1 : c0;
-                    if (wn) stack[top++] = near0 ? c0 : c1;
-                    __syncwarp();
+                    const uint32_t e = __shfl_sync(kFull, li < 32 ? v0 : v1, li & 31) & (uint32_t)(kWideLeaves - 1);
+                    ++li;
+                    leaf = stack[e];
+                    if (leaf + 1u == own || leaf == own + 1u) continue;  // scanned already
+                    ++st_nodes;
+                    // the lane's node_lb of the leaf, from the kept box
+                    const float(*const bx)[kWideLeaves] = s_bx[w];
+                    const float gx = fmaxf(fmaxf(__fsub_rn(bx[0][e], P.x), __fsub_rn(P.x, bx[D][e])), 0.f);
+                    const float gy = fmaxf(fmaxf(__fsub_rn(bx[1][e], P.y), __fsub_rn(P.y, bx[D + 1][e])), 0.f);
+                    float gz = 0.f;
+                    if constexpr (D == 3) gz = fmaxf(fmaxf(__fsub_rn(bx[2][e], P.z), __fsub_rn(P.z, bx[5][e])), 0.f);
+                    need = __ballot_sync(kFull, wanted(d2_of<D>(gx, gy, gz)));
+                } else {
+                    // the walk, up to the next leaf some lane wants
+                    for (;;) {
+                        if (top == 0) {
+                            if (dv <= 1) {
+                                phase = kDone;
+                                break;
+                            }
+                            const uint32_t sib = dv ^ 1u;
+                            dv >>= 1;
+                            ++st_nodes;
+                            if (!__any_sync(kFull, wanted(node_lb(sib)))) continue;
+                            __syncwarp();
+                            stack[0] = sib;
+                            top = 1;
+                            __syncwarp();
+                        }
+                        const uint32_t node = stack[--top];
+                        ++st_nodes;
+                        if (node >= L) {
+                            const uint32_t lf = node - L;
+                            // single point sets reach the walk after the neighbours
+                            if (!CL && (lf + 1u == own || lf == own + 1u)) continue;
+                            // bounds re-checked: they may have shrunk since the push
+                            need = __ballot_sync(kFull, wanted(node_lb(node)));
+                            if (need) {
+                                leaf = lf;
+                                break;
+                            }
+                            continue;
+                        }
+                        const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                        const float l0 = node_lb(c0), l1 = node_lb(c1);
+                        const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
+                        // the child nearer to the warp's nearest lane is searched next
+                        const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
+                        const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
+                        const bool near0 = m0 <= m1;
+                        const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
+                        __syncwarp();  // every lane has read the popped entry
+                        if (wf) stack[top++] = near0 ? c1 : c0;
+                        if (wn) stack[top++] = near0 ? c0 : c1;
+                        __syncwarp();
+                    }
                 }
+                if (need) scan_leaf(leaf, need, staged);
             }
             if constexpr (!LEARN) break;
             // A learned radius that held fewer than K points: the list is not
