@@ -495,6 +495,48 @@ __global__ void __launch_bounds__(kWideWarps * 32) k_cnns_w(const CnnsArgs a)
     }
 }
 
+// Gathers of k_cnns_c and k_knn_first: nodes the frontier may hold, leaves a
+// gather may collect.
+constexpr int kWideFront = 128;
+constexpr int kWideLeaves = 64;
+
+// Ascending bitonic sort of 32 keys, one per lane.
+__device__ __forceinline__ uint32_t bitonic_sort32(uint32_t v, int lane)
+{
+#pragma unroll 1
+    for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll 1
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const uint32_t o = __shfl_xor_sync(kFull, v, j);
+            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+            v = keep_min ? min(v, o) : max(v, o);
+        }
+    return v;
+}
+
+// Ascending bitonic sort of 64 keys: element e is v0 of lane e (e < 32) or
+// v1 of lane e - 32.
+__device__ __forceinline__ void bitonic_sort64(uint32_t& v0, uint32_t& v1, int lane)
+{
+#pragma unroll 1
+    for (int k = 2; k <= 64; k <<= 1)
+#pragma unroll 1
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j == 32) {  // k == 64: the halves of each lane, ascending
+                const uint32_t lo = min(v0, v1), hi = max(v0, v1);
+                v0 = lo;
+                v1 = hi;
+            } else {
+                const uint32_t o0 = __shfl_xor_sync(kFull, v0, j), o1 = __shfl_xor_sync(kFull, v1, j);
+                const bool lower = (lane & j) == 0;
+                // e & k for e = lane and e = lane + 32 (they differ only for k == 32)
+                const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
+                v0 = lower == up0 ? min(v0, o0) : max(v0, o0);
+                v1 = lower == up1 ? min(v1, o1) : max(v1, o1);
+            }
+        }
+}
+
 // Component search for long query lists: one warp per 32 consecutive
 // queries, walking the tree together (k_knn_first's traversal), each lane
 // keeping its own nearest point outside its component.
@@ -532,6 +574,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     __shared__ uint32_t s_lab[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
+    // the gather's frontier and its leaves' sort keys; none for point batches
+    __shared__ uint32_t s_fr[kKnnWarps][CL ? 1 : kWideFront];
+    __shared__ uint32_t s_lk[kKnnWarps][CL ? 1 : kWideLeaves];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float4* const pt = s_pt[w];
     uint32_t* const labs = s_lab[w];
@@ -649,51 +694,184 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
             refresh_cb();
         };
 
-        // the warp's own leaf (lane 0's query's) first, then bottom-up: every
-        // other leaf lies in exactly one sibling subtree of its ancestors
+        // Leaves come from a warp-uniform state machine, so that every one
+        // goes through the single scan below.  Default: the warp's own leaf
+        // (lane 0's query's) first, then bottom-up -- every other leaf lies in
+        // exactly one sibling subtree of its ancestors -- a node entered when
+        // any lane wants it.
+        //
+        // Single-component warps (in late rounds most warps: 32 points of one
+        // big component) gather first, as k_knn_first does: the own leaf and
+        // the ancestors' siblings are tested one per lane in one step, then 32
+        // nodes a step, against the queries' box grown by B (the largest
+        // bound of any lane; here every lane's bound is its component's key)
+        // and the shared label (a node holding only the component is
+        // skipped).  The box-to-box bound never exceeds a lane's node_lb, so
+        // nothing a lane wants is dropped, and a node it drops is beyond every
+        // lane's key: its bound joins every lane's cut.  Often nothing is
+        // gathered at all: a point deep inside its component learns in one
+        // step that no outside point is nearer than the key, where the
+        // depth-first walk tests the ancestors' siblings one by one.
+        // Gathered leaves are scanned nearest first.  A frontier or leaf list
+        // that overflows falls back to the depth-first walk.
         const uint32_t own = __shfl_sync(kFull, me, 0) >> 5;
-        {
-            const float lo = node_lb(L + own);
-            note(lo);
-            const uint32_t need = __ballot_sync(kFull, wanted(lo));
-            if (need) scan_leaf(own, need);
-        }
-        for (uint32_t v = L + own; v > 1; v >>= 1) {
-            const uint32_t sib = v ^ 1u;
-            ++st_nodes;
-            {
-                const float ls = node_lb(sib);
-                note(ls);
-                if (!__any_sync(kFull, wanted(ls))) continue;
+        enum { kOwn, kGathered, kWalk, kDone };
+        int phase = kOwn;
+        int li = 0, nl = 0;
+        uint32_t v0 = ~0u, v1 = ~0u;  // the gathered leaves' sorted keys
+        const unsigned vmask = __ballot_sync(kFull, valid);
+        if (!vmask) phase = kDone;  // no lane can hold its component's minimum
+        if constexpr (!CL) {
+            const uint32_t lab0 = __shfl_sync(kFull, labp, vmask ? __ffs(vmask) - 1 : 0);
+            // rescaled coordinates are >= +0: their bits order as the values
+            const uint32_t sx = __float_as_uint(P.x), sy = __float_as_uint(P.y), sz = __float_as_uint(P.z);
+            const bool neg = ((sx | sy | sz) >> 31) != 0u;
+            const float B = __uint_as_float(__reduce_max_sync(kFull, __float_as_uint(fmaxf(fminf(bd, cb), 0.f))));
+            if (vmask && B < INFINITY && __all_sync(kFull, !valid || (labp == lab0 && !neg))) {
+                float4 qlo, qhi;
+                qlo.x = __uint_as_float(__reduce_min_sync(kFull, valid ? sx : 0x7f800000u));
+                qlo.y = __uint_as_float(__reduce_min_sync(kFull, valid ? sy : 0x7f800000u));
+                qlo.z = __uint_as_float(__reduce_min_sync(kFull, valid ? sz : 0x7f800000u));
+                qhi.x = __uint_as_float(__reduce_max_sync(kFull, valid ? sx : 0u));
+                qhi.y = __uint_as_float(__reduce_max_sync(kFull, valid ? sy : 0u));
+                qhi.z = __uint_as_float(__reduce_max_sync(kFull, valid ? sz : 0u));
+                uint32_t* const fr = s_fr[w];
+                uint32_t* const lk = s_lk[w];
+                const unsigned below = (1u << lane) - 1u;
+                const int depth = 31 - __clz(L);  // levels under the root (L is a power of two)
+                __syncwarp();
+                if (lane < depth) fr[lane] = ((L + own) >> lane) ^ 1u;
+                if (lane == depth) fr[lane] = L + own;
+                __syncwarp();
+                int top = depth + 1;
+                float dropped = INFINITY;  // smallest bound of a node dropped by distance (this lane's tests)
+                bool ok = true;
+                while (top > 0) {
+                    const int take = min(top, 32);
+                    top -= take;
+                    ++st_nodes;
+                    uint32_t node = 0;
+                    float lb = INFINITY;
+                    if (lane < take) {
+                        node = fr[top + lane];
+                        if (__ldg(&nlab[node]) != lab0) {
+                            const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                            const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, qhi.x), __fsub_rn(qlo.x, hi.x)), 0.f);
+                            const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, qhi.y), __fsub_rn(qlo.y, hi.y)), 0.f);
+                            const float gz =
+                                D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, qhi.z), __fsub_rn(qlo.z, hi.z)), 0.f) : 0.f;
+                            lb = d2_of<D>(gx, gy, gz);
+                        }
+                    }
+                    const bool want = lb <= B, is_leaf = node >= L;
+                    if (!want) dropped = fminf(dropped, lb);  // +inf: empty or the component's own
+                    const unsigned ml = __ballot_sync(kFull, want && is_leaf);
+                    const unsigned mi = __ballot_sync(kFull, want && !is_leaf);
+                    const int nlf = __popc(ml), nin = __popc(mi);
+                    if (nl + nlf > kWideLeaves || top + 2 * nin > kWideFront) {
+                        ok = false;
+                        break;
+                    }
+                    __syncwarp();  // every lane has read its entry: the pushes may overwrite it
+                    if (want && is_leaf) {
+                        const int e = nl + __popc(ml & below);
+                        stack[e] = node - L;
+                        lk[e] = (__float_as_uint(lb) & ~(uint32_t)(kWideLeaves - 1)) | (uint32_t)e;
+                    }
+                    if (want && !is_leaf) {
+                        const int e = top + 2 * __popc(mi & below);
+                        fr[e] = 2u * node;
+                        fr[e + 1] = 2u * node + 1u;
+                    }
+                    nl += nlf;
+                    top += 2 * nin;
+                    __syncwarp();
+                }
+                if (ok) {
+                    // every lane's cut takes the nodes dropped by distance
+                    const float dmin = __uint_as_float(__reduce_min_sync(kFull, __float_as_uint(dropped)));
+                    if (valid) cut = fminf(cut, dmin);
+                    v0 = lane < nl ? lk[lane] : ~0u;
+                    v1 = lane + 32 < nl ? lk[lane + 32] : ~0u;
+                    if (nl > 32) bitonic_sort64(v0, v1, lane);
+                    else if (nl > 1) v0 = bitonic_sort32(v0, lane);
+                    phase = kGathered;
+                } else {
+                    nl = 0;
+                }
             }
-            int top = 0;
-            stack[top++] = sib;
-            while (top > 0) {
-                const uint32_t node = stack[--top];
-                ++st_nodes;
-                if (node >= L) {
-                    // bounds re-checked: they may have shrunk since the push
-                    const float lb = node_lb(node);
-                    note(lb);
-                    const uint32_t need = __ballot_sync(kFull, wanted(lb));
-                    if (need) scan_leaf(node - L, need);
+        }
+        uint32_t dv = L + own;  // the walk: the ancestor whose sibling comes next
+        int top = 0;            // the walk's stack depth
+        while (phase != kDone) {
+            uint32_t leaf = 0, need = 0;
+            if (phase == kOwn) {
+                const float lo = node_lb(L + own);
+                note(lo);
+                leaf = own;
+                need = __ballot_sync(kFull, wanted(lo));
+                phase = kWalk;
+            } else if (phase == kGathered) {
+                if (li >= nl) {
+                    phase = kDone;
                     continue;
                 }
-                const uint32_t c0 = 2 * node, c1 = c0 + 1;
-                const float l0 = node_lb(c0), l1 = node_lb(c1);
-                note(l0);
-                note(l1);
-                const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
-                // the child nearer to the warp's nearest lane is searched next
-                const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
-                const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
-                const bool near0 = m0 <= m1;
-                const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
-                __syncwarp();  // every lane has read the popped entry
-                if (wf) stack[top++] = near0 ? c1 : c0;
-                if (wn) stack[top++] = near0 ? c0 : c1;
-                __syncwarp();
+                const uint32_t e = __shfl_sync(kFull, li < 32 ? v0 : v1, li & 31) & (uint32_t)(kWideLeaves - 1);
+                ++li;
+                leaf = stack[e];
+                ++st_nodes;
+                const float lb = node_lb(L + leaf);
+                note(lb);
+                need = __ballot_sync(kFull, wanted(lb));
+            } else {
+                // the walk, up to the next leaf some lane wants
+                for (;;) {
+                    if (top == 0) {
+                        if (dv <= 1) {
+                            phase = kDone;
+                            break;
+                        }
+                        const uint32_t sib = dv ^ 1u;
+                        dv >>= 1;
+                        ++st_nodes;
+                        const float ls = node_lb(sib);
+                        note(ls);
+                        if (!__any_sync(kFull, wanted(ls))) continue;
+                        __syncwarp();
+                        stack[0] = sib;
+                        top = 1;
+                        __syncwarp();
+                    }
+                    const uint32_t node = stack[--top];
+                    ++st_nodes;
+                    if (node >= L) {
+                        // bounds re-checked: they may have shrunk since the push
+                        const float lb = node_lb(node);
+                        note(lb);
+                        need = __ballot_sync(kFull, wanted(lb));
+                        if (need) {
+                            leaf = node - L;
+                            break;
+                        }
+                        continue;
+                    }
+                    const uint32_t c0 = 2 * node, c1 = c0 + 1;
+                    const float l0 = node_lb(c0), l1 = node_lb(c1);
+                    note(l0);
+                    note(l1);
+                    const bool w0 = __any_sync(kFull, wanted(l0)), w1 = __any_sync(kFull, wanted(l1));
+                    // the child nearer to the warp's nearest lane is searched next
+                    const uint32_t m0 = __reduce_min_sync(kFull, __float_as_uint(l0));
+                    const uint32_t m1 = __reduce_min_sync(kFull, __float_as_uint(l1));
+                    const bool near0 = m0 <= m1;
+                    const bool wn = near0 ? w0 : w1, wf = near0 ? w1 : w0;
+                    __syncwarp();  // every lane has read the popped entry
+                    if (wf) stack[top++] = near0 ? c1 : c0;
+                    if (wn) stack[top++] = near0 ? c0 : c1;
+                    __syncwarp();
+                }
             }
+            if (need) scan_leaf(leaf, need);
         }
         bool record = false;
         if (valid) {
@@ -728,47 +906,6 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
             }
         }
     }
-}
-
-// Wide walk of k_knn_first: nodes one level may hold, leaves it may gather.
-constexpr int kWideFront = 128;
-constexpr int kWideLeaves = 64;
-
-// Ascending bitonic sort of 32 keys, one per lane.
-__device__ __forceinline__ uint32_t bitonic_sort32(uint32_t v, int lane)
-{
-#pragma unroll 1
-    for (int k = 2; k <= 32; k <<= 1)
-#pragma unroll 1
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            const uint32_t o = __shfl_xor_sync(kFull, v, j);
-            const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-            v = keep_min ? min(v, o) : max(v, o);
-        }
-    return v;
-}
-
-// Ascending bitonic sort of 64 keys: element e is v0 of lane e (e < 32) or
-// v1 of lane e - 32.
-__device__ __forceinline__ void bitonic_sort64(uint32_t& v0, uint32_t& v1, int lane)
-{
-#pragma unroll 1
-    for (int k = 2; k <= 64; k <<= 1)
-#pragma unroll 1
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            if (j == 32) {  // k == 64: the halves of each lane, ascending
-                const uint32_t lo = min(v0, v1), hi = max(v0, v1);
-                v0 = lo;
-                v1 = hi;
-            } else {
-                const uint32_t o0 = __shfl_xor_sync(kFull, v0, j), o1 = __shfl_xor_sync(kFull, v1, j);
-                const bool lower = (lane & j) == 0;
-                // e & k for e = lane and e = lane + 32 (they differ only for k == 32)
-                const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
-                v0 = lower == up0 ? min(v0, o0) : max(v0, o0);
-                v1 = lower == up1 ? min(v1, o1) : max(v1, o1);
-            }
-        }
 }
 
 // Round 1 with neighbour lists: each point's kKnn nearest other points (its
