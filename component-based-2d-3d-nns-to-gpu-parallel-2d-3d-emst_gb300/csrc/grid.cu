@@ -152,7 +152,8 @@ __global__ void k_minmax_final(const float* __restrict__ part, int nblk, int64_t
 // Rescale (SolutionEMST.cu:361-364) + Hilbert cell key.
 template <int D>
 __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const NormParams* __restrict__ np,
-                              float* __restrict__ scaled, uint64_t* __restrict__ key, uint32_t* __restrict__ idx)
+                              float* __restrict__ scaled, uint64_t* __restrict__ key, uint32_t* __restrict__ idx,
+                              int pack)
 {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -165,18 +166,31 @@ __global__ void k_rescale_key(const float* __restrict__ in, int64_t n, const Nor
         float qf = fminf(fmaxf(__fmul_rn(s, qs), 0.f), (float)((1u << kCellBits<D>) - 1u));
         cell[c] = (uint32_t)qf;
     }
-    key[i] = hilbert_index<D, kCellBits<D>>(cell);
-    idx[i] = (uint32_t)i;
+    const uint64_t h = hilbert_index<D, kCellBits<D>>(cell);
+    if (pack > 0) {
+        key[i] = (h << pack) | (uint64_t)i;  // the index rides in the low bits
+    } else {
+        key[i] = h;
+        idx[i] = (uint32_t)i;
+    }
 }
 
-// Gather rescaled points into leaf order; .w carries the input id.
+// Gather rescaled points into leaf order; .w carries the input id.  With
+// packed sorted keys (index in the low `pack` bits) the order is read from
+// them and written to perm.
 template <int D>
-__global__ void k_gather(const float* __restrict__ scaled, const uint32_t* __restrict__ perm, int64_t n,
-                         float4* __restrict__ sp, uint32_t* __restrict__ pos0)
+__global__ void k_gather(const float* __restrict__ scaled, const uint64_t* __restrict__ packed, int pack,
+                         uint32_t* __restrict__ perm, int64_t n, float4* __restrict__ sp, uint32_t* __restrict__ pos0)
 {
     int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= n) return;
-    uint32_t i = perm[j];
+    uint32_t i;
+    if (packed) {
+        i = (uint32_t)(packed[j] & ((1ull << pack) - 1ull));
+        perm[j] = i;
+    } else {
+        i = perm[j];
+    }
     if (i == 0) *pos0 = (uint32_t)j;
     float4 v;
     v.x = scaled[(int64_t)i * D + 0];
@@ -306,34 +320,46 @@ cudaError_t grid_build(Ctx& c)
     if ((e = c.ensure(c.nhi, (size_t)2 * c.L)) != cudaSuccess) return e;
     if ((e = c.ensure(c.nid, (size_t)2 * c.L)) != cudaSuccess) return e;
 
+    // bits of a point index; with the cell key's they fit one 64-bit word up
+    // to 2^24 points (2^25 in 3D)
+    const int end_bit = grid_sort_end_bit(D);
+    int ib = 0;
+    while (ib < 32 && (1ll << ib) < n) ++ib;
+    const int pack = ib > 0 && ib + end_bit <= 64 ? ib : 0;
     if (D == 2) {
         k_minmax_part<2><<<nblk, kRedThreads, 0, s>>>(c.in, n, c.part.p, c.ctr.p);
         k_minmax_final<2><<<1, kRedThreads, 0, s>>>(c.part.p, nblk, n, c.norm.p);
-        k_rescale_key<2><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p);
+        k_rescale_key<2><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p, pack);
     } else {
         k_minmax_part<3><<<nblk, kRedThreads, 0, s>>>(c.in, n, c.part.p, c.ctr.p);
         k_minmax_final<3><<<1, kRedThreads, 0, s>>>(c.part.p, nblk, n, c.norm.p);
-        k_rescale_key<3><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p);
+        k_rescale_key<3><<<blocks_for(n, 256), 256, 0, s>>>(c.in, n, c.norm.p, c.scaled.p, c.mkey.p, c.perm.p, pack);
     }
-    // Radix sort of the cell keys (only the significant bits).
-    const int end_bit = grid_sort_end_bit(D);
+    // Radix sort of the cell keys (only the significant bits): keys alone
+    // when the index fits beside the key in 64 bits, else (key, index) pairs
     const size_t tmp = radix_scratch_bytes(n, end_bit);
     if ((e = c.ensure(c.sort_tmp, tmp)) != cudaSuccess) return e;
     bool in_alt = false;
-    if ((e = radix_sort_pairs(c.mkey.p, c.mkey_alt.p, c.perm.p, c.perm_alt.p, n, end_bit, c.sort_tmp.p, tmp,
-                              &c.ctr.p->err, &in_alt, s)) != cudaSuccess)
-        return e;
+    if (pack > 0)
+        e = radix_sort_keys(c.mkey.p, c.mkey_alt.p, n, pack, end_bit, c.sort_tmp.p, tmp, &c.ctr.p->err, &in_alt, s);
+    else
+        e = radix_sort_pairs(c.mkey.p, c.mkey_alt.p, c.perm.p, c.perm_alt.p, n, end_bit, c.sort_tmp.p, tmp,
+                             &c.ctr.p->err, &in_alt, s);
+    if (e != cudaSuccess) return e;
     c.launches += 2 + radix_passes(end_bit);
     if (in_alt) {
         std::swap(c.mkey.p, c.mkey_alt.p);
         std::swap(c.mkey.cap, c.mkey_alt.cap);
-        std::swap(c.perm.p, c.perm_alt.p);
-        std::swap(c.perm.cap, c.perm_alt.cap);
+        if (pack == 0) {
+            std::swap(c.perm.p, c.perm_alt.p);
+            std::swap(c.perm.cap, c.perm_alt.cap);
+        }
     }
+    const uint64_t* packed = pack > 0 ? c.mkey.p : nullptr;
     if (D == 2)
-        k_gather<2><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
+        k_gather<2><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, packed, pack, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
     else
-        k_gather<3><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
+        k_gather<3><<<blocks_for(n, 256), 256, 0, s>>>(c.scaled.p, packed, pack, c.perm.p, n, c.sp.p, &c.ctr.p->pos0);
     c.launches += 4;
     return leaf_tree(c);
 }

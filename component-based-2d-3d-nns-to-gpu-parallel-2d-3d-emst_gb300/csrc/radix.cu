@@ -13,8 +13,8 @@
 //                    values through shared memory so that each digit's run
 //                    is written contiguously.
 //
-// Bytes per pair and pass: 12 read + 12 written; the histogram reads the keys
-// once more.  A block waits only on tiles whose tickets came before its own,
+// Bytes per pair and pass: 12 read + 12 written (8 + 8 for keys alone); the
+// histogram reads the keys once more.  A block waits only on tiles whose tickets came before its own,
 // so every block it waits on is already running; each wait is still bounded
 // and reports through *err instead of spinning on.
 #include "radix.cuh"
@@ -61,14 +61,15 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_tmp)
 }
 
 __global__ void __launch_bounds__(kRadixThreads)
-    k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, int passes, uint32_t* __restrict__ hist)
+    k_radix_hist(const uint64_t* __restrict__ keys, uint32_t n, int begin_bit, int passes, uint32_t* __restrict__ hist)
 {
     __shared__ uint32_t s_h[kRadixMaxPasses][kRadixBins];
     for (int i = threadIdx.x; i < kRadixMaxPasses * kRadixBins; i += blockDim.x) (&s_h[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint64_t k = keys[i];
-        for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][(uint32_t)(k >> (kRadixBits * p)) & 0xffu], 1u);
+        for (int p = 0; p < passes; ++p)
+            atomicAdd(&s_h[p][(uint32_t)(k >> (begin_bit + kRadixBits * p)) & 0xffu], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * kRadixBins; i += blockDim.x) {
@@ -86,7 +87,8 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_offsets(int passes, uin
     }
 }
 
-__global__ void __launch_bounds__(kRadixThreads)
+template <bool VALUES>
+__global__ void __launch_bounds__(kRadixThreads, VALUES ? 2 : 3)
     k_radix_pass(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                  uint32_t* __restrict__ vout, uint32_t n, int shift, const uint32_t* __restrict__ goff,
                  unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket, uint32_t* __restrict__ err)
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(kRadixThreads)
     for (int i = 0; i < kRadixItems; ++i) {
         const uint32_t idx = wbase + (uint32_t)i * 32u + (uint32_t)lane;
         k[i] = idx < n ? kin[idx] : 0ull;
-        v[i] = idx < n ? vin[idx] : 0u;
+        if constexpr (VALUES) v[i] = idx < n ? vin[idx] : 0u;
     }
 #pragma unroll
     for (int i = 0; i < kRadixItems; ++i) {
@@ -195,6 +197,7 @@ __global__ void __launch_bounds__(kRadixThreads)
     }
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < tile_n; j += kRadixThreads) kout[s_gbase[s_dig[j]] + j] = s_buf[j];
+    if constexpr (!VALUES) return;
     __syncthreads();
     // 5. the values the same way
     uint32_t* const s_val = reinterpret_cast<uint32_t*>(s_buf);
@@ -227,16 +230,18 @@ Layout layout(int64_t n, int end_bit)
 
 size_t radix_scratch_bytes(int64_t n, int end_bit) { return layout(n, end_bit).total; }
 
-cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt, int64_t n,
-                             int end_bit, void* scratch, size_t scratch_bytes, uint32_t* err, bool* in_alt,
-                             cudaStream_t s)
+namespace {
+
+cudaError_t radix_sort(uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt, int64_t n,
+                       int begin_bit, int nbits, void* scratch, size_t scratch_bytes, uint32_t* err, bool* in_alt,
+                       cudaStream_t s)
 {
     *in_alt = false;
-    if (n <= 1 || end_bit <= 0) return cudaSuccess;
-    if (end_bit > 64 || n > (int64_t)0x7fffffff) return cudaErrorInvalidValue;
-    const Layout l = layout(n, end_bit);
+    if (n <= 1 || nbits <= 0) return cudaSuccess;
+    if (begin_bit < 0 || begin_bit + nbits > 64 || n > (int64_t)0x7fffffff) return cudaErrorInvalidValue;
+    const Layout l = layout(n, nbits);
     if (!scratch || scratch_bytes < l.total) return cudaErrorInvalidValue;
-    const int passes = radix_passes(end_bit);
+    const int passes = radix_passes(nbits);
     const uint32_t tiles = (uint32_t)((n + kRadixTile - 1) / kRadixTile);
     unsigned char* base = static_cast<unsigned char*>(scratch);
     uint32_t* hist = reinterpret_cast<uint32_t*>(base + l.hist);
@@ -249,21 +254,44 @@ cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* keys_alt, uint32_t* vals,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t hblocks = std::min<uint64_t>(((uint64_t)n + kRadixThreads - 1) / kRadixThreads,
                                                 (uint64_t)std::max(sms, 1) * 4);
-    k_radix_hist<<<(unsigned)hblocks, kRadixThreads, 0, s>>>(keys, (uint32_t)n, passes, hist);
+    k_radix_hist<<<(unsigned)hblocks, kRadixThreads, 0, s>>>(keys, (uint32_t)n, begin_bit, passes, hist);
     k_radix_offsets<<<1, kRadixThreads, 0, s>>>(passes, hist);
     uint64_t* ki = keys;
     uint64_t* ko = keys_alt;
     uint32_t* vi = vals;
     uint32_t* vo = vals_alt;
     for (int p = 0; p < passes; ++p) {
-        k_radix_pass<<<tiles, kRadixThreads, 0, s>>>(ki, vi, ko, vo, (uint32_t)n, kRadixBits * p,
-                                                     hist + p * kRadixBins, status + (size_t)p * tiles * kRadixBins,
-                                                     tickets + p, err);
+        const int shift = begin_bit + kRadixBits * p;
+        if (vals)
+            k_radix_pass<true><<<tiles, kRadixThreads, 0, s>>>(ki, vi, ko, vo, (uint32_t)n, shift, hist + p * kRadixBins,
+                                                               status + (size_t)p * tiles * kRadixBins, tickets + p,
+                                                               err);
+        else
+            k_radix_pass<false><<<tiles, kRadixThreads, 0, s>>>(ki, nullptr, ko, nullptr, (uint32_t)n, shift,
+                                                                hist + p * kRadixBins,
+                                                                status + (size_t)p * tiles * kRadixBins, tickets + p,
+                                                                err);
         std::swap(ki, ko);
         std::swap(vi, vo);
     }
     *in_alt = (passes & 1) != 0;
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* keys_alt, uint32_t* vals, uint32_t* vals_alt, int64_t n,
+                             int end_bit, void* scratch, size_t scratch_bytes, uint32_t* err, bool* in_alt,
+                             cudaStream_t s)
+{
+    if (!vals || !vals_alt) return cudaErrorInvalidValue;
+    return radix_sort(keys, keys_alt, vals, vals_alt, n, 0, end_bit, scratch, scratch_bytes, err, in_alt, s);
+}
+
+cudaError_t radix_sort_keys(uint64_t* keys, uint64_t* keys_alt, int64_t n, int begin_bit, int nbits, void* scratch,
+                            size_t scratch_bytes, uint32_t* err, bool* in_alt, cudaStream_t s)
+{
+    return radix_sort(keys, keys_alt, nullptr, nullptr, n, begin_bit, nbits, scratch, scratch_bytes, err, in_alt, s);
 }
 
 }  // namespace emst

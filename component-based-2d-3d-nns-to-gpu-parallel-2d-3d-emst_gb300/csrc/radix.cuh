@@ -29,6 +29,13 @@ inline int radix_passes(int end_bit) { return (end_bit + kRadixBits - 1) / kRadi
 // Bytes of scratch radix_sort_pairs needs for n pairs and keys of end_bit bits.
 size_t radix_scratch_bytes(int64_t n, int end_bit);
 
+// Sorts keys[0, n) alone by bits [begin_bit, begin_bit + nbits) (lower bits
+// ride along; higher bits must be zero), stably; the scratch is
+// radix_scratch_bytes(n, nbits).  For keys that carry their value in the low
+// bits.  *in_alt as below.
+cudaError_t radix_sort_keys(uint64_t* keys, uint64_t* keys_alt, int64_t n, int begin_bit, int nbits, void* scratch,
+                            size_t scratch_bytes, uint32_t* err, bool* in_alt, cudaStream_t s);
+
 // Sorts keys[0, n) (only bits [0, end_bit) are compared; higher bits must be
 // zero) and vals[0, n) along with them, stably.  keys_alt / vals_alt are
 // buffers of the same sizes; *in_alt tells where the sorted pairs ended
