@@ -130,6 +130,7 @@ __global__ void k_hook(const uint32_t* __restrict__ roots2, const DevCounters* d
                        int32_t* __restrict__ eround, uint32_t* __restrict__ n_edges, uint32_t n,
                        uint32_t* __restrict__ err)
 {
+    __shared__ uint32_t s_cnt[33];
     const uint32_t total = dc->n_roots;
     const int round = dc->round;
     const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
@@ -155,20 +156,12 @@ __global__ void k_hook(const uint32_t* __restrict__ roots2, const DevCounters* d
                 v = max(ow, oq);
             }
         }
-        const unsigned act = __activemask();
-        const unsigned m = __ballot_sync(act, emit);
-        if (m) {
-            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-            uint32_t b = 0;
-            if (lane == leader) b = atomicAdd(n_edges, (uint32_t)__popc(m));
-            b = __shfl_sync(act, b, leader);
-            const uint32_t k = b + __popc(m & ((1u << lane) - 1u));
-            if (emit && k + 1 >= n) atomicOr(err, 4u);  // more than n - 1 edges: internal error
-            if (emit && k + 1 < n) {
-                edges[2 * (uint64_t)k] = (int32_t)u;
-                edges[2 * (uint64_t)k + 1] = (int32_t)v;
-                eround[k] = round;
-            }
+        const uint32_t k = block_reserve(emit, n_edges, s_cnt);
+        if (emit && k + 1 >= n) atomicOr(err, 4u);  // more than n - 1 edges: internal error
+        if (emit && k + 1 < n) {
+            edges[2 * (uint64_t)k] = (int32_t)u;
+            edges[2 * (uint64_t)k + 1] = (int32_t)v;
+            eround[k] = round;
         }
     }
 }
@@ -230,6 +223,7 @@ __global__ void k_compact_roots(uint32_t* __restrict__ roots2, DevCounters* dc, 
     const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
     uint32_t* roots_next = roots2 + (size_t)(dc->rpar ^ 1u) * n;
     uint32_t* n_roots_next = &dc->n_roots;
+    __shared__ uint32_t s_cnt[33];
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool keep = false;
@@ -243,7 +237,8 @@ __global__ void k_compact_roots(uint32_t* __restrict__ roots2, DevCounters* dc, 
                 if (clb) clb[c] = 0x7f800000u;  // +inf
             }
         }
-        warp_append(keep, c, roots_next, n_roots_next);
+        const uint32_t slot = block_reserve(keep, n_roots_next, s_cnt);
+        if (keep) roots_next[slot] = c;
     }
 }
 

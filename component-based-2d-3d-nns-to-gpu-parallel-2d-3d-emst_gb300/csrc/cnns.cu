@@ -117,6 +117,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
     // writes every result this pass would, so the pass has nothing to do
     if (klist && r == 1) return;
     const bool lists = klist && r >= 2;
+    __shared__ uint32_t s_cnt[33];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool is_dirty = false, record = false;
@@ -195,7 +196,8 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
             }
         }
         if (p < n) dflag[p] = is_dirty ? 1 : 0;
-        warp_append(record, p, prov, n_prov);
+        const uint32_t slot = block_reserve(record, n_prov, s_cnt);
+        if (record) prov[slot] = p;
     }
 }
 

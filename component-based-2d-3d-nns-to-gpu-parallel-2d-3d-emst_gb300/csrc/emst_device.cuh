@@ -194,4 +194,31 @@ __device__ __forceinline__ uint64_t hilbert_index(uint32_t (&x)[3])
     return (spread2(x[0]) << 1) | spread2(x[1]);
 }
 
+// Block-aggregated slot reservation through counter *cnt: one atomic per
+// block instead of one per warp.  A single counter taking an atomic from every
+// warp of a pass over 10^7 points serialises at the L2 (round 1 hooks and
+// keeps millions of roots).  Every thread of the block calls it (the callers'
+// loops run the same trip count across the block, full warps); s_cnt has 33
+// entries.  Returns the slot of a thread with pred.
+__device__ __forceinline__ uint32_t block_reserve(bool pred, uint32_t* cnt, uint32_t* s_cnt)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_cnt[w] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int i = 0; i < nw; ++i) {
+            const uint32_t c = s_cnt[i];
+            s_cnt[i] = t;
+            t += c;
+        }
+        s_cnt[32] = t ? atomicAdd(cnt, t) : 0u;
+    }
+    __syncthreads();
+    const uint32_t slot = s_cnt[32] + s_cnt[w] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    __syncthreads();  // s_cnt is reused by the next call
+    return slot;
+}
+
 }  // namespace emst
