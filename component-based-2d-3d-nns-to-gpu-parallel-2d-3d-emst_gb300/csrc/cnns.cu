@@ -118,21 +118,33 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
     if (klist && r == 1) return;
     const bool lists = klist && r >= 2;
     __shared__ uint32_t s_cnt[33];
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // the next iteration's partner, label and bound are loaded one iteration
+    // ahead: the pass is bound by chains of dependent loads
+    uint32_t p_next = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t q_next = p_next < n ? selq[p_next] : kNone, lp_next = p_next < n ? lab[p_next] : 0u;
+    uint32_t lb_next = p_next < n ? __float_as_uint(lbp[p_next]) : 0u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t p = base + threadIdx.x;
+        const uint32_t q = q_next, lp0 = lp_next, lb0 = lb_next;
+        p_next = p + stride;
+        if (p_next < n) {
+            q_next = selq[p_next];
+            lp_next = lab[p_next];
+            lb_next = __float_as_uint(lbp[p_next]);
+        }
         bool is_dirty = false, record = false;
         uint64_t key = kNoKey;
         uint32_t lp = 0;
         if (p < n) {
-            const uint32_t q = selq[p];
-            lp = lab[p];
+            lp = lp0;
             // round 2 with lists: the partner is list entry 0, the round-1
             // edge, inside the component for certain (k_knn_first set the
             // cursor past it)
             if (!(lists && r == 2) && q != kNone && lab[q] != lp) {
                 key = selkey[p];
             } else {
-                uint32_t lb = __float_as_uint(lbp[p]);
+                uint32_t lb = lb0;
                 if (lists && lb != 0x7f800000u) {
                     // the first neighbour outside the component is the exact
                     // nearest outside point: every closer point precedes it.
@@ -196,8 +208,11 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
             }
         }
         if (p < n) dflag[p] = is_dirty ? 1 : 0;
-        const uint32_t slot = block_reserve(record, n_prov, s_cnt);
-        if (record) prov[slot] = p;
+        // late rounds record few points: one vote skips the reservation
+        if (__syncthreads_or(record)) {
+            const uint32_t slot = block_reserve(record, n_prov, s_cnt);
+            if (record) prov[slot] = p;
+        }
     }
 }
 
