@@ -57,23 +57,39 @@ __global__ void __launch_bounds__(1024)
     __shared__ uint32_t s[kLeavesPerBlock];
     const uint32_t first = blockIdx.x * span;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t l = w; l < span; l += blockDim.x >> 5) {
-        const uint32_t c = first + l;
-        uint32_t out = kEmpty;
-        if (c < nchunk) {
+    // four leaves per warp and step, their loads issued together (each leaf
+    // is a chain of two dependent loads: the label, then its root)
+    constexpr int kU = 4;
+    const uint32_t nw = blockDim.x >> 5;
+    for (uint32_t l0 = w; l0 < span; l0 += kU * nw) {
+        uint32_t my[kU];
+        bool v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t l = l0 + (uint32_t)u * nw, c = first + l;
             const uint32_t j = c * 32 + lane;
-            const bool v = j < n;
-            uint32_t my = v ? lab[j] : 0u;
-            if (par && v) {
-                my = __ldcg(&par[my]);
-                lab[j] = my;
-            }
-            const uint32_t l0 = __shfl_sync(kFull, my, 0);
-            out = __all_sync(kFull, !v || my == l0) ? l0 : kMixed;
+            v[u] = l < span && c < nchunk && j < n;
+            my[u] = v[u] ? lab[j] : 0u;
         }
-        if (lane == 0) {
-            s[l] = out;
-            nlab[L + c] = out;
+        if (par) {
+#pragma unroll
+            for (int u = 0; u < kU; ++u)
+                if (v[u]) my[u] = __ldcg(&par[my[u]]);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t l = l0 + (uint32_t)u * nw, c = first + l;
+            if (l >= span) break;  // warp-uniform
+            if (par && v[u]) lab[c * 32 + lane] = my[u];
+            uint32_t out = kEmpty;
+            if (c < nchunk) {
+                const uint32_t f = __shfl_sync(kFull, my[u], 0);
+                out = __all_sync(kFull, !v[u] || my[u] == f) ? f : kMixed;
+            }
+            if (lane == 0) {
+                s[l] = out;
+                nlab[L + c] = out;
+            }
         }
     }
     __syncthreads();
@@ -475,26 +491,53 @@ __global__ void __launch_bounds__(kSelThreads)
     load_flags(flag, p0, n, f);
     uint32_t mine = 0, later = 0;
     bool changed = false;
+    bool any = false;
 #pragma unroll
-    for (int k = 0; k < kSelItems; ++k) {
-        const uint32_t p = p0 + k;
-        unsigned char nf = f[k];
-        if (f[k] && stage != 2) {
-            const uint32_t l = lab[p];
-            const float lb = lbp[p];
-            const uint64_t key = __ldcg(&ckey[l]);
-            const float cb = key == kNoKey ? INFINITY : __uint_as_float((uint32_t)(key >> 32));
-            if (stage == 0) {
-                nf = 0;
-                if (!(lb > cb)) nf = lb > factor * __uint_as_float(__ldcg(&clb[l])) ? 2 : 1;
-                later += nf == 2;
-            } else {
-                nf = (f[k] == 2 && !(lb > cb)) ? kSelPicked : 0;
+    for (int k = 0; k < kSelItems; ++k) any |= f[k] != 0;
+    if (any && stage != 2) {
+        // labels and bounds in two 16-byte loads each (p0 is a multiple of 8),
+        // then every flagged point's component key and bound at once: the
+        // gathers of the eight points overlap instead of queueing
+        uint32_t l[kSelItems];
+        float lb[kSelItems];
+        if (p0 + kSelItems <= n) {
+            const uint4 a = *reinterpret_cast<const uint4*>(lab + p0), b = *reinterpret_cast<const uint4*>(lab + p0 + 4);
+            const float4 c = *reinterpret_cast<const float4*>(lbp + p0), d = *reinterpret_cast<const float4*>(lbp + p0 + 4);
+            l[0] = a.x; l[1] = a.y; l[2] = a.z; l[3] = a.w; l[4] = b.x; l[5] = b.y; l[6] = b.z; l[7] = b.w;
+            lb[0] = c.x; lb[1] = c.y; lb[2] = c.z; lb[3] = c.w; lb[4] = d.x; lb[5] = d.y; lb[6] = d.z; lb[7] = d.w;
+        } else {
+#pragma unroll
+            for (int k = 0; k < kSelItems; ++k) {
+                l[k] = f[k] ? lab[p0 + k] : 0u;
+                lb[k] = f[k] ? lbp[p0 + k] : 0.f;
             }
         }
-        changed |= nf != f[k];
-        f[k] = nf;
-        const int o = list_of(stage, nf, two);
+        uint64_t key[kSelItems];
+        uint32_t cl[kSelItems];
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k) {
+            key[k] = f[k] ? __ldcg(&ckey[l[k]]) : kNoKey;
+            cl[k] = f[k] && stage == 0 ? __ldcg(&clb[l[k]]) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < kSelItems; ++k) {
+            if (!f[k]) continue;
+            const float cb = key[k] == kNoKey ? INFINITY : __uint_as_float((uint32_t)(key[k] >> 32));
+            unsigned char nf;
+            if (stage == 0) {
+                nf = 0;
+                if (!(lb[k] > cb)) nf = lb[k] > factor * __uint_as_float(cl[k]) ? 2 : 1;
+                later += nf == 2;
+            } else {
+                nf = (f[k] == 2 && !(lb[k] > cb)) ? kSelPicked : 0;
+            }
+            changed |= nf != f[k];
+            f[k] = nf;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kSelItems; ++k) {
+        const int o = list_of(stage, f[k], two);
         mine += o == 1 ? 1u : (o == 2 ? 0x10000u : 0u);
     }
     if (changed) {
