@@ -571,6 +571,8 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     uint64_t* __restrict__ ckey = a.ckey;
     constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
     __shared__ float4 s_pt[kKnnWarps][32];
+    // the staged leaf's coordinates again, one row per axis (packed d2)
+    __shared__ __align__(16) float s_ax[kKnnWarps][D][32];
     __shared__ uint32_t s_lab[kKnnWarps][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
@@ -637,28 +639,46 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
             ++st_leaves;
             __syncwarp();  // the previous leaf's reads are done
             if ((uint32_t)lane < m) {
-                pt[lane] = __ldg(&sp[b + lane]);
+                const float4 c = __ldg(&sp[b + lane]);
+                pt[lane] = c;
+                s_ax[w][0][lane] = c.x;
+                s_ax[w][1][lane] = c.y;
+                if constexpr (D == 3) s_ax[w][2][lane] = c.z;
                 labs[lane] = __ldg(&lab[b + lane]);
                 if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
             } else {
-                // past the last point: NaN coordinates fail every d2 <= bound test
+                // past the last point: NaN coordinates fail every d2 <= bound
+                // test, and so does the +inf of the rows (d2 = +inf)
                 pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, __uint_as_float(~0u));
+                s_ax[w][0][lane] = INFINITY;
+                s_ax[w][1][lane] = 0.f;
+                if constexpr (D == 3) s_ax[w][2][lane] = 0.f;
                 labs[lane] = kEmpty;
                 if constexpr (CL) s_cl[w][lane] = ~0u;
             }
             __syncwarp();
             if (__popc(need) > kKnnDense) {
-#pragma unroll 8
-                for (int j = 0; j < 32; ++j) {
-                    const float4 c = pt[j];
-                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                    bool ok = d2 <= bd && labs[j] != labp;
-                    if constexpr (CL) ok = ok && s_cl[w][j] == qc;
-                    const uint32_t id = __float_as_uint(c.w);
-                    const bool better = ok && (d2 < bd || id < bo);  // (d2, id) order; ok has d2 <= bd
-                    bd = better ? d2 : bd;
-                    bo = better ? id : bo;
-                    bs = better ? b + (uint32_t)j : bs;
+                // two candidates' d2 per packed step (bit for bit d2_of),
+                // then each in turn against the lane's best
+#pragma unroll 4
+                for (int h = 0; h < 16; ++h) {
+                    const f32x2 cx = reinterpret_cast<const f32x2*>(s_ax[w][0])[h];
+                    const f32x2 cy = reinterpret_cast<const f32x2*>(s_ax[w][1])[h];
+                    const f32x2 cz = D == 3 ? reinterpret_cast<const f32x2*>(s_ax[w][D - 1])[h] : 0ull;
+                    const f32x2 d2p =
+                        d2_of2<D>(cx, cy, cz, f2_dup(P.x), f2_dup(P.y), f2_dup(D == 3 ? P.z : 0.f));
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int j = 2 * h + u;
+                        const float d2 = __uint_as_float(u ? (uint32_t)(d2p >> 32) : (uint32_t)d2p);
+                        bool ok = d2 <= bd && labs[j] != labp;
+                        if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                        const uint32_t id = __float_as_uint(pt[j].w);
+                        const bool better = ok && (d2 < bd || id < bo);  // (d2, id) order; ok has d2 <= bd
+                        bd = better ? d2 : bd;
+                        bo = better ? id : bo;
+                        bs = better ? b + (uint32_t)j : bs;
+                    }
                 }
             } else {
                 const float4 c = pt[lane];
@@ -942,6 +962,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
     constexpr int kWStack = 64;  // a tree of 32-bit node ids is < 33 levels deep
     static_assert(kWideLeaves <= kWStack && kWideFront >= 32, "the wide walk's leaf list and frontier");
     __shared__ float4 s_pt[kKnnWarps][32];
+    // the staged leaf's coordinates again, one row per axis, read two
+    // candidates at a time by the packed marking (x of a missing point +inf)
+    __shared__ __align__(16) float s_ax[kKnnWarps][D][32];
     __shared__ uint32_t s_cl[kKnnWarps][CL ? 32 : 1];
     __shared__ uint32_t s_stack[kKnnWarps][kWStack];
     // the wide walk's frontier, its leaves' sort keys and boxes (lo then hi
@@ -1003,14 +1026,30 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         auto stage_leaf = [&](uint32_t b, uint32_t m) {
             __syncwarp();  // the previous leaf's reads are done
             if ((uint32_t)lane < m) {
-                pt[lane] = __ldg(&sp[b + lane]);
+                const float4 c = __ldg(&sp[b + lane]);
+                pt[lane] = c;
+                s_ax[w][0][lane] = c.x;
+                s_ax[w][1][lane] = c.y;
+                if constexpr (D == 3) s_ax[w][2][lane] = c.z;
                 if constexpr (CL) s_cl[w][lane] = __ldg(&pcloud[b + lane]);
             } else {
-                // past the last point: NaN coordinates fail every d2 <= bound test
+                // past the last point: NaN coordinates fail every d2 <= bound
+                // test; +inf in the rows gives d2 = +inf, beyond every bound
                 pt[lane] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);
+                s_ax[w][0][lane] = INFINITY;
+                s_ax[w][1][lane] = 0.f;
+                if constexpr (D == 3) s_ax[w][2][lane] = 0.f;
                 if constexpr (CL) s_cl[w][lane] = ~0u;
             }
             __syncwarp();
+        };
+        // d2 of candidates 2h and 2h + 1 of the staged leaf (packed, bit for
+        // bit d2_of)
+        auto pair_d2 = [&](int h) -> f32x2 {
+            const f32x2 cx = reinterpret_cast<const f32x2*>(s_ax[w][0])[h];
+            const f32x2 cy = reinterpret_cast<const f32x2*>(s_ax[w][1])[h];
+            const f32x2 cz = D == 3 ? reinterpret_cast<const f32x2*>(s_ax[w][D - 1])[h] : 0ull;
+            return d2_of2<D>(cx, cy, cz, f2_dup(P.x), f2_dup(P.y), f2_dup(D == 3 ? P.z : 0.f));
         };
         auto scan_leaf = [&](uint32_t leaf, uint32_t need, bool staged) {
             const uint32_t b = leaf * 32;
@@ -1018,16 +1057,25 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             ++st_leaves;
             if (!staged) stage_leaf(b, m);
             uint32_t mask = 0;
-            if (__popc(need) > kKnnDense) {
+            if (__popc(need) > kKnnDenseFirst) {
+                if constexpr (CL) {
 #pragma unroll 8
-                for (int j = 0; j < 32; ++j) {
-                    const float4 c = pt[j];
-                    const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                    // in a batch, a point of another cloud is no candidate
-                    // (lanes may hold different clouds)
-                    bool ok = d2 <= bd;
-                    if constexpr (CL) ok = ok && s_cl[w][j] == qc;
-                    mask |= (ok ? 1u : 0u) << j;
+                    for (int j = 0; j < 32; ++j) {
+                        const float4 c = pt[j];
+                        const float d2 = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
+                        // in a batch, a point of another cloud is no candidate
+                        // (lanes may hold different clouds)
+                        const bool ok = d2 <= bd && s_cl[w][j] == qc;
+                        mask |= (ok ? 1u : 0u) << j;
+                    }
+                } else {
+                    // two candidates per packed step; the sign of bd - d2
+                    // marks the rejected ones
+                    const f32x2 b2 = f2_dup(bd);
+                    uint32_t rej = 0;
+#pragma unroll 8
+                    for (int h = 15; h >= 0; --h) rej = reject_append2(rej, b2, pair_d2(h));
+                    mask = ~rej;
                 }
                 // round 1: the query's component is the query alone
                 if (leaf == (me >> 5)) mask &= ~(1u << (me & 31u));
@@ -1097,18 +1145,22 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
             float t[K];
 #pragma unroll
             for (int i = 0; i < K; ++i) t[i] = INFINITY;
-#pragma unroll 4
-            for (int j = 0; j < 32; ++j) {
-                const float4 c = pt[j];
-                float d = d2_of<D>(__fsub_rn(c.x, P.x), __fsub_rn(c.y, P.y), __fsub_rn(c.z, P.z));
-                bool ok = j != self && d <= FLT_MAX;  // NaN padding and the query itself are out
-                if constexpr (CL) ok = ok && s_cl[w][j] == qc;
-                d = ok ? d : INFINITY;
+#pragma unroll 2
+            for (int h = 0; h < 16; ++h) {
+                const f32x2 d2 = pair_d2(h);
 #pragma unroll
-                for (int i = 0; i < K; ++i) {
-                    const float lo = fminf(t[i], d);
-                    d = fmaxf(t[i], d);
-                    t[i] = lo;
+                for (int u = 0; u < 2; ++u) {
+                    const int j = 2 * h + u;
+                    float d = __uint_as_float(u ? (uint32_t)(d2 >> 32) : (uint32_t)d2);
+                    bool ok = j != self && d <= FLT_MAX;  // padding (+inf) and the query itself are out
+                    if constexpr (CL) ok = ok && s_cl[w][j] == qc;
+                    d = ok ? d : INFINITY;
+#pragma unroll
+                    for (int i = 0; i < K; ++i) {
+                        const float lo = fminf(t[i], d);
+                        d = fmaxf(t[i], d);
+                        t[i] = lo;
+                    }
                 }
             }
             tk = t[K - 1];

@@ -39,7 +39,8 @@ constexpr int kKnn = EMST_ROUND1_NEIGHBOURS;
 constexpr int kNumKnnLengths = 4;
 constexpr int kKnnLengths[kNumKnnLengths] = {4, 5, 6, 8};
 constexpr int kKnnWarps = 8;  // warps per block of k_knn_first
-constexpr int kKnnDense = 16;  // k_knn_first: lanes wanting a leaf above which all lanes test all its points
+constexpr int kKnnDense = 16;  // k_cnns_c: lanes wanting a leaf above which all lanes test all its points
+constexpr int kKnnDenseFirst = 11;  // the same for k_knn_first (packed marking; swept 8, 11, 16)
 constexpr int kWideWarps = 8;  // warps per block of k_cnns_w
 constexpr int kWideFan = 5;    // k_cnns_w: levels a traversal step descends (32 nodes, one per lane)
 // longest query list k_cnns_w takes (warp per query); longer lists fill the GPU

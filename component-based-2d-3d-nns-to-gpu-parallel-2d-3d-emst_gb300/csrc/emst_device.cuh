@@ -45,6 +45,62 @@ __device__ __forceinline__ float d2_of(float dx, float dy, float dz)
     return r;
 }
 
+// Packed FP32 pairs (sm_100 family: add/sub/mul/fma .rn.f32x2).  Each half is
+// the IEEE round-to-nearest operation of the scalar instruction, denormals
+// kept, so a pair gives bit for bit the two scalar results of d2_of: two
+// candidates' distances for the price of one instruction per step.
+using f32x2 = uint64_t;  // low word: the first value, high word: the second
+
+__device__ __forceinline__ f32x2 f2_dup(float v)
+{
+    const uint64_t b = __float_as_uint(v);
+    return b | (b << 32);
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c)
+{
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// d2_of for two candidates (x, y, z pairs) against one point (P duplicated).
+template <int D>
+__device__ __forceinline__ f32x2 d2_of2(f32x2 cx, f32x2 cy, f32x2 cz, f32x2 px, f32x2 py, f32x2 pz)
+{
+    const f32x2 dx = f2_sub(cx, px), dy = f2_sub(cy, py);
+    f32x2 r = f2_fma(dy, dy, f2_mul(dx, dx));
+    if (D == 3) {
+        const f32x2 dz = f2_sub(cz, pz);
+        r = f2_fma(dz, dz, r);
+    }
+    return r;
+}
+
+// Bits "d2 > bound" of two candidates, shifted into a mask from the bottom:
+// the sign bit of bound - d2.  IEEE subtraction with denormals gives zero only
+// for equal operands (+0 under round to nearest), so the sign is set exactly
+// when d2 > bound, including d2 = +inf and a bound of -1.  The second value's
+// bit goes in first, so after pairs 15, 14, ..., 0 bit j of the mask is
+// candidate j; the candidates within the bound are the complement.
+__device__ __forceinline__ uint32_t reject_append2(uint32_t mask, f32x2 bound2, f32x2 d2)
+{
+    const f32x2 s = f2_sub(bound2, d2);
+    mask = __funnelshift_l((uint32_t)(s >> 32), mask, 1);
+    return __funnelshift_l((uint32_t)s, mask, 1);
+}
+
 // Region bit mask of a candidate at offset d = q - p (general path: ties and zeros).
 template <int D>
 __device__ __forceinline__ uint32_t region_mask(float dx, float dy, float dz)
