@@ -379,7 +379,8 @@ cudaError_t boruvka_flatten(Ctx& c)
     }
     k_flatten_begin<<<1, 1, 0, c.stream>>>(d);
     k_compact_roots<<<list_grid(c.n_roots), 256, 0, c.stream>>>(c.roots.p, d, n, c.par.p, c.ckey.p, c.cmax.p,
-                                                                c.search_mode == 0 ? c.clb.p : nullptr);
+                                                                c.search_mode == 0 && c.clb_used() ? c.clb.p
+                                                                                                    : nullptr);
     k_flatten_end<<<1, 1, 0, c.stream>>>(d);
     c.launches += 5;
     return cudaGetLastError();

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(1024) k_node_labels_top(uint32_t top, uint32_t
 
 // Points whose previous partner is still outside their component re-submit
 // it; the others go to the dirty list and fold their lower bound into their
-// component's minimum bound clb.
+// component's minimum bound clb (when a first-pass rule reads it: clb set).
 __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* __restrict__ selq,
                         uint64_t* __restrict__ selkey, float* __restrict__ lbp, uint64_t* __restrict__ ckey,
                         uint32_t* __restrict__ clb, unsigned char* __restrict__ dflag, uint32_t* __restrict__ prov,
@@ -200,7 +200,7 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     // lbp = +inf: no point outside the component exists (in a batch,
                     // the cloud is one component), and components only grow
                     is_dirty = lb != 0x7f800000u;
-                    if (is_dirty && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
+                    if (is_dirty && clb && lb < __ldcg(&clb[lp])) atomicMin(&clb[lp], lb);
                 }
             }
         }
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(kSelThreads)
 #pragma unroll
         for (int k = 0; k < kSelItems; ++k) {
             key[k] = f[k] ? __ldcg(&ckey[l[k]]) : kNoKey;
-            cl[k] = f[k] && stage == 0 ? __ldcg(&clb[l[k]]) : 0u;
+            cl[k] = f[k] && stage == 0 && clb ? __ldcg(&clb[l[k]]) : 0u;
         }
 #pragma unroll
         for (int k = 0; k < kSelItems; ++k) {
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(kSelThreads)
             unsigned char nf;
             if (stage == 0) {
                 nf = 0;
-                if (!(lb[k] > cb)) nf = lb[k] > factor * __uint_as_float(cl[k]) ? 2 : 1;
+                if (!(lb[k] > cb)) nf = clb && lb[k] > factor * __uint_as_float(cl[k]) ? 2 : 1;
                 later += nf == 2;
             } else {
                 nf = (f[k] == 2 && !(lb[k] > cb)) ? kSelPicked : 0;
@@ -637,7 +637,8 @@ cudaError_t select_list(Ctx& c, int stage, float factor, uint32_t* list1, uint32
     const uint32_t tiles = (uint32_t)((c.n + kSelTile - 1) / kSelTile);
     const bool two = list2 != nullptr;
     k_sel_count<<<tiles, kSelThreads, 0, c.stream>>>(skip, (uint32_t)c.n, stage, c.dflag.p, c.lab.p, c.lbp.p, c.ckey.p,
-                                                     c.clb.p, factor, two, c.sel_tiles.p, stats);
+                                                     c.clb_used() ? c.clb.p : nullptr, factor, two, c.sel_tiles.p,
+                                                     stats);
     k_sel_scan<<<1, kScanThreads, 0, c.stream>>>(skip, tiles, c.sel_tiles.p, cnt1, two ? cnt2 : nullptr);
     k_sel_write<<<tiles, kSelThreads, 0, c.stream>>>(skip, (uint32_t)c.n, stage, c.dflag.p, two, c.sel_tiles.p, tiles,
                                                      list1, list2);
@@ -714,9 +715,12 @@ cudaError_t cnns_init(Ctx& c)
         c.launches++;
     }
     k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.selq.p, (uint32_t)c.n, kNone);
-    k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
+    if (c.clb_used()) {
+        k_fill_u32<<<blocks_for(c.n, 256), 256, 0, c.stream>>>(c.clb.p, (uint32_t)c.n, 0x7f800000u);
+        c.launches++;
+    }
     cudaMemsetAsync(c.lbp.p, 0, n * sizeof(float), c.stream);
-    c.launches += 2;
+    c.launches++;
     // node labels of the initial forest; each round's flatten refreshes them
     return cnns_node_labels(c);
 }
@@ -728,7 +732,8 @@ cudaError_t cnns_select(Ctx& c)
     DevCounters* d = c.ctr.p;  // n_dirty, n_dirty2, n_prov were zeroed by the round tick
     const bool knn = c.knn_seed && !c.cnns_warp;
     k_reuse<<<list_grid(c.n), 256, 0, c.stream>>>((uint32_t)c.n, c.lab.p, c.selq.p, c.selkey.p, c.lbp.p, c.ckey.p,
-                                                  c.clb.p, c.dflag.p, c.prov.p, &d->n_prov, &d->round,
+                                                  c.clb_used() ? c.clb.p : nullptr, c.dflag.p, c.prov.p, &d->n_prov,
+                                                  &d->round,
                                                   knn ? c.klist.p : nullptr, c.kcur.p, c.perm.p, c.knn_k);
     c.launches++;
     // query lists in leaf order: a warp's 32 queries are neighbours, so their

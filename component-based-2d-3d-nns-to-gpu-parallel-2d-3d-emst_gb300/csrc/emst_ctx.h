@@ -177,6 +177,9 @@ struct Ctx {
     // (one pass); with the query lists compacted before each pass, deferring
     // measured slower on GB300 for every factor tried (1.0001 .. 16)
     float first_pass_factor = INFINITY;
+    // The per-root smallest bound clb is read only by a finite first-pass
+    // factor and by the warp search's deferral; otherwise no pass keeps it.
+    bool clb_used() const { return cnns_warp || !std::isinf(first_pass_factor); }
     // round 1 keeps each point's knn_k nearest (k_knn_first); later rounds take
     // the first entry outside the component without a search (k_reuse)
     bool knn_seed = true;
