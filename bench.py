@@ -138,8 +138,9 @@ def cpu_baseline(pts, threads, sample_n, seed=0, with_edges=False):
     idx = rng.choice(len(pts), min(sample_n, len(pts)), replace=False)
     sub = np.ascontiguousarray(pts[np.sort(idx)])
     O.set_threads(threads)
-    sp, _, _, _ = O.rescale(sub)
+    # timed from the raw points, as the GPU solve is (rescale included)
     t0 = time.perf_counter()
+    sp, _, _, _ = O.rescale(sub)
     r = O.emst(sp, "faithful")
     dt = time.perf_counter() - t0
     assert len(r.edges) == len(sub) - 1
@@ -290,6 +291,12 @@ def learned_leg(E, args, local, stream, settings, flush, dev_pts, d_uv, d_len, n
                     "network); the top-level value is the autotuned plain form (the library default)"}
 
 
+def workload_config(workload, n, dim):
+    """The benchmark configuration, the same dict in both arms."""
+    return {"workload": workload, "n": n, "dim": dim,
+            "l2": "GPU arm: 512 MB buffer written between timed steps; working set > 129 MB L2"}
+
+
 def run_reference(args, pts, dim):
     """The CPU restatement of the reference's path, all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -308,7 +315,7 @@ def run_reference(args, pts, dim):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": args.workload, "n": len(pts), "dim": dim},
+            "data": "synthetic", "config": workload_config(args.workload, len(pts), dim),
             "cpu_baseline": {"value": value, "unit": "Mpoints/s", "cores": threads, "kind": "port",
                              "cpu_model": cpu_model(),
                              "sample": "%d random points of %s per step (CPU restatement of the reference's "
@@ -541,14 +548,14 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": args.workload, "n": n, "dim": dim, "rounds": rounds,
-                           "search": {0: "component: round-1 neighbour lists (warp per 32 queries); later "
-                                         "rounds by query-list length: warp per query, thread per query, "
-                                         "warp per 32 queries", 1: "static region table",
-                                      2: "component, warp per 32 queries"}[args.mode],
-                           "l2": "512 MB buffer written between timed steps; working set > 129 MB L2",
-                           "launch_shape": launch_shape,
-                           "parallelism": "replicas" if world > 1 else "single"},
+                "config": workload_config(args.workload, n, dim),
+                "settings": {"rounds": rounds,
+                             "search": {0: "component: round-1 neighbour lists (warp per 32 queries); later "
+                                           "rounds by query-list length: warp per query, thread per query, "
+                                           "warp per 32 queries", 1: "static region table",
+                                        2: "component, warp per 32 queries"}[args.mode],
+                             "launch_shape": launch_shape,
+                             "parallelism": "replicas" if world > 1 else "single"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                              "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,

@@ -135,19 +135,28 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
     const bool lists = klist && r >= 2;
     __shared__ uint32_t s_cnt[33];
     const uint32_t stride = gridDim.x * blockDim.x;
-    // the next iteration's partner, label and bound are loaded one iteration
-    // ahead: the pass is bound by chains of dependent loads
+    // The pass is bound by chains of dependent loads.  The next iteration's
+    // partner, label, bound and list cursor are loaded one iteration ahead;
+    // then the partner's label, the list entry at the cursor, the point's own
+    // input id and its key are loaded together (the last three only where
+    // they may be used), so a point waits on four levels of loads, not six.
     uint32_t p_next = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t q_next = p_next < n ? selq[p_next] : kNone, lp_next = p_next < n ? lab[p_next] : 0u;
-    uint32_t lb_next = p_next < n ? __float_as_uint(lbp[p_next]) : 0u;
+    uint32_t q_next = kNone, lp_next = 0u, lb_next = 0u, j0_next = 0u;
+    if (p_next < n) {
+        q_next = selq[p_next];
+        lp_next = lab[p_next];
+        lb_next = __float_as_uint(lbp[p_next]);
+        if (lists) j0_next = kcur[p_next];
+    }
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t p = base + threadIdx.x;
-        const uint32_t q = q_next, lp0 = lp_next, lb0 = lb_next;
+        const uint32_t q = q_next, lp0 = lp_next, lb0 = lb_next, j0 = j0_next;
         p_next = p + stride;
         if (p_next < n) {
             q_next = selq[p_next];
             lp_next = lab[p_next];
             lb_next = __float_as_uint(lbp[p_next]);
+            if (lists) j0_next = kcur[p_next];
         }
         bool is_dirty = false, record = false;
         uint64_t key = kNoKey;
@@ -157,8 +166,14 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
             // round 2 with lists: the partner is list entry 0, the round-1
             // edge, inside the component for certain (k_knn_first set the
             // cursor past it)
-            if (!(lists && r == 2) && q != kNone && lab[q] != lp) {
-                key = selkey[p];
+            const bool has_q = !(lists && r == 2) && q != kNone;
+            const bool walk = lists && lb0 != 0x7f800000u && (int)j0 < knn_k;
+            const uint32_t lq = has_q ? lab[q] : lp;
+            const uint64_t sk = has_q ? selkey[p] : kNoKey;
+            const uint64_t k0 = walk ? klist[(size_t)j0 * n + p] : ~0ull;
+            const uint32_t op = walk ? perm[p] : 0u;
+            if (has_q && lq != lp) {
+                key = sk;
             } else {
                 uint32_t lb = lb0;
                 if (lists && lb != 0x7f800000u) {
@@ -168,17 +183,17 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                     // component in an earlier round and stay inside
                     // (components only grow); their d2 is already in lbp.
                     bool full = true;
-                    const int j0 = kcur[p];
-                    int j = j0;
+                    int j = (int)j0;
                     for (; j < knn_k; ++j) {
-                        const uint64_t kj = klist[(size_t)j * n + p];  // d2 bits << 32 | position
+                        // d2 bits << 32 | position
+                        const uint64_t kj = j == (int)j0 ? k0 : klist[(size_t)j * n + p];
                         const uint32_t qj = (uint32_t)kj;
                         if (qj == kNone) {
                             full = false;
                             break;
                         }
                         if (lab[qj] != lp) {
-                            const uint32_t mn = min(perm[p], perm[qj]);
+                            const uint32_t mn = min(op, perm[qj]);
                             key = (kj & 0xffffffff00000000ull) | mn;
                             selq[p] = qj;
                             selkey[p] = key;
@@ -187,8 +202,8 @@ __global__ void k_reuse(uint32_t n, const uint32_t* __restrict__ lab, uint32_t* 
                         }
                         lb = max(lb, (uint32_t)(kj >> 32));  // non-negative floats order as their bits
                     }
-                    if (j != j0) kcur[p] = (unsigned char)j;
-                    if (key == kNoKey && (j != j0 || !full)) {
+                    if (j != (int)j0) kcur[p] = (unsigned char)j;
+                    if (key == kNoKey && (j != (int)j0 || !full)) {
                         // none outside: a full list bounds the distance from below;
                         // a short one held every other point of the cloud
                         // (an exhausted list, j0 == knn_k, adds nothing new)
