@@ -105,24 +105,61 @@ __global__ void k_select(const uint32_t* __restrict__ act, const uint32_t* __res
     }
 }
 
+// Per component, among its provisional winners (points whose key reached
+// the component's slot), the one with the smallest (larger input id of the
+// edge, position): the (d2, min id, max id) order's winner.  Four winners per
+// thread and iteration, each level of their loads issued together (label,
+// partner, key and input id; then the component's key and the partner's id).
 __global__ void k_resolve(const uint32_t* __restrict__ prov, const uint32_t* __restrict__ n_prov,
                           const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
                           const uint64_t* __restrict__ ckey, const uint32_t* __restrict__ selq,
-                          const uint64_t* __restrict__ selkey, uint64_t* __restrict__ cmax)
+                          const uint64_t* __restrict__ selkey, uint64_t* __restrict__ cmax,
+                          const int* __restrict__ skip_round)
 {
+    // round 1 with neighbour lists: the list build wrote every winner slot
+    if (skip_round && *skip_round == 1) return;
+    constexpr int kU = 4;
     const uint32_t total = *n_prov;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const uint32_t p = prov[i];
-        const uint32_t lp = lab[p];
-        const uint32_t q = selq[p];
-        // a result without a partner (not certified) cannot be the winner; if
-        // it held the component's key the hook reports it (no winner found)
-        if (selkey[p] != ckey[lp] || q == kNoPartner) continue;
-        const uint32_t mx = max(perm[p], perm[q]);
-        atomicMin((unsigned long long*)&cmax[lp], (unsigned long long)(((uint64_t)mx << 32) | p));
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < total; i0 += kU * stride) {
+        uint32_t p[kU], lp[kU], q[kU], op[kU], oq[kU];
+        uint64_t sk[kU], ck[kU];
+        bool v[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = i0 + (uint32_t)u * stride;
+            v[u] = i < total;
+            p[u] = v[u] ? prov[i] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            lp[u] = v[u] ? lab[p[u]] : 0u;
+            q[u] = v[u] ? selq[p[u]] : kNoPartner;
+            sk[u] = v[u] ? selkey[p[u]] : kNoKey;
+            op[u] = v[u] ? perm[p[u]] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            ck[u] = v[u] ? ckey[lp[u]] : 0ull;
+            oq[u] = v[u] && q[u] != kNoPartner ? perm[q[u]] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            // a result without a partner (not certified) cannot be the winner; if
+            // it held the component's key the hook reports it (no winner found)
+            if (!v[u] || sk[u] != ck[u] || q[u] == kNoPartner) continue;
+            const uint32_t mx = max(op[u], oq[u]);
+            atomicMin((unsigned long long*)&cmax[lp[u]], (unsigned long long)(((uint64_t)mx << 32) | p[u]));
+        }
     }
 }
 
+// Every root with an outgoing edge hooks onto the root across it (a mutual
+// pair: the root holding the lower input id stays) and emits the edge once.
+// Four roots per thread and iteration, each level of their chains of
+// dependent loads issued together: the root's key and winner; the winner's
+// partner and input id; the partner's root and input id; that root's key and
+// winner.
 __global__ void k_hook(const uint32_t* __restrict__ roots2, const DevCounters* dc,
                        const uint32_t* __restrict__ lab, const uint32_t* __restrict__ perm,
                        const uint64_t* __restrict__ ckey, const uint64_t* __restrict__ cmax,
@@ -131,37 +168,64 @@ __global__ void k_hook(const uint32_t* __restrict__ roots2, const DevCounters* d
                        uint32_t* __restrict__ err)
 {
     __shared__ uint32_t s_cnt[33];
+    constexpr int kU = 4;
     const uint32_t total = dc->n_roots;
     const int round = dc->round;
     const uint32_t* roots = roots2 + (size_t)dc->rpar * n;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        bool emit = false;
-        uint32_t u = 0, v = 0;
-        if (i < total) {
-            const uint32_t c = roots[i];
-            const uint64_t ck = ckey[c];
-            const uint64_t cm = cmax[c];
-            if (ck != kNoKey && (cm == kNoKey || (uint32_t)cm >= n)) {
-                atomicOr(err, 2u);  // a root with an edge key but no winner: internal error
-            } else if (ck != kNoKey) {
-                const uint32_t w = (uint32_t)cm;
-                const uint32_t q = selq[w];
-                const uint32_t cq = lab[q];
-                const bool mutual = ckey[cq] == ck && (cmax[cq] >> 32) == (cm >> 32);
-                const uint32_t ow = perm[w], oq = perm[q];
-                if (!mutual || ow > oq) par[c] = cq;
-                emit = !mutual || ow < oq;
-                u = min(ow, oq);
-                v = max(ow, oq);
-            }
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // block-uniform trip count: block_reserve synchronises the block
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += kU * stride) {
+        uint32_t c[kU], w[kU], q[kU], ow[kU], cq[kU], oq[kU];
+        uint64_t ck[kU], cm[kU], kq[kU], mq[kU];
+        bool v[kU], go[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t i = base + (uint32_t)u * stride + threadIdx.x;
+            v[u] = i < total;
+            c[u] = v[u] ? roots[i] : 0u;
         }
-        const uint32_t k = block_reserve(emit, n_edges, s_cnt);
-        if (emit && k + 1 >= n) atomicOr(err, 4u);  // more than n - 1 edges: internal error
-        if (emit && k + 1 < n) {
-            edges[2 * (uint64_t)k] = (int32_t)u;
-            edges[2 * (uint64_t)k + 1] = (int32_t)v;
-            eround[k] = round;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            ck[u] = v[u] ? ckey[c[u]] : kNoKey;
+            cm[u] = v[u] ? cmax[c[u]] : kNoKey;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            go[u] = ck[u] != kNoKey && cm[u] != kNoKey && (uint32_t)cm[u] < n;
+            w[u] = go[u] ? (uint32_t)cm[u] : 0u;
+            q[u] = go[u] ? selq[w[u]] : 0u;
+            ow[u] = go[u] ? perm[w[u]] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            cq[u] = go[u] ? lab[q[u]] : 0u;
+            oq[u] = go[u] ? perm[q[u]] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            kq[u] = go[u] ? ckey[cq[u]] : kNoKey;
+            mq[u] = go[u] ? cmax[cq[u]] : kNoKey;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            bool emit = false;
+            uint32_t a = 0, b = 0;
+            if (v[u] && ck[u] != kNoKey && !go[u]) {
+                atomicOr(err, 2u);  // a root with an edge key but no winner: internal error
+            } else if (go[u]) {
+                const bool mutual = kq[u] == ck[u] && (mq[u] >> 32) == (cm[u] >> 32);
+                if (!mutual || ow[u] > oq[u]) par[c[u]] = cq[u];
+                emit = !mutual || ow[u] < oq[u];
+                a = min(ow[u], oq[u]);
+                b = max(ow[u], oq[u]);
+            }
+            const uint32_t k = block_reserve(emit, n_edges, s_cnt);
+            if (emit && k + 1 >= n) atomicOr(err, 4u);  // more than n - 1 edges: internal error
+            if (emit && k + 1 < n) {
+                edges[2 * (uint64_t)k] = (int32_t)a;
+                edges[2 * (uint64_t)k + 1] = (int32_t)b;
+                eround[k] = round;
+            }
         }
     }
 }
@@ -423,8 +487,10 @@ cudaError_t boruvka_select(Ctx& c)
 cudaError_t boruvka_resolve(Ctx& c)
 {
     DevCounters* d = c.ctr.p;
+    // the round-1 list build (component search) fills the winner slots itself
+    const int* skip = (c.search_mode == 0 && c.knn_seed && !c.cnns_warp) ? &d->round : nullptr;
     k_resolve<<<list_grid(c.n_act), 256, 0, c.stream>>>(c.prov.p, &d->n_prov, c.lab.p, c.perm.p, c.ckey.p, c.selq.p,
-                                                         c.selkey.p, c.cmax.p);
+                                                         c.selkey.p, c.cmax.p, skip);
     c.launches++;
     return cudaGetLastError();
 }

@@ -806,6 +806,7 @@ cudaError_t cnns_select(Ctx& c)
             }
             const int shape = search_shape_of(c);
             a.knn_k = c.knn_k;
+            a.cmax = c.cmax.p;
             if (knn && pass == 1) {  // round 1 only (decided on the device)
                 // the learned proposal steers the list build's starting bound
                 // (single clouds); traces record the plain build

@@ -584,11 +584,19 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
     uint32_t* const labs = s_lab[w];
     uint32_t* const stack = s_stack[w];
     const uint32_t stride = gridDim.x * kKnnWarps * 32;
+    // the list entry of the next iteration is loaded one iteration ahead
+    auto entry = [&](uint32_t b) -> uint32_t {
+        const uint32_t qi = b + lane;
+        const uint32_t qs = qi < total ? qi : b;
+        return qs < n1 ? a.list[qs] : a.list2[qs - n1];
+    };
+    uint32_t me_next = 0;
+    if ((blockIdx.x * kKnnWarps + w) * 32 < total) me_next = entry((blockIdx.x * kKnnWarps + w) * 32);
     for (uint32_t base0 = (blockIdx.x * kKnnWarps + w) * 32; base0 < total; base0 += stride) {
         const uint32_t qi = base0 + lane;
         const bool listed = qi < total;
-        const uint32_t qs = listed ? qi : base0;
-        const uint32_t me = qs < n1 ? a.list[qs] : a.list2[qs - n1];
+        const uint32_t me = me_next;
+        if (base0 + stride < total) me_next = entry(base0 + stride);
         const uint32_t labp = listed ? a.lab[me] : kEmpty;
         const float lb0 = listed ? a.lbp[me] : 0.f;
         float cb = INFINITY;
@@ -773,15 +781,17 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_cnns_c(const CnnsArgs a)
                     uint32_t node = 0;
                     float lb = INFINITY;
                     if (lane < take) {
+                        // label and box loaded together (one wait per step,
+                        // not two); a node holding only the component is
+                        // skipped
                         node = fr[top + lane];
-                        if (__ldg(&nlab[node]) != lab0) {
-                            const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
-                            const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, qhi.x), __fsub_rn(qlo.x, hi.x)), 0.f);
-                            const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, qhi.y), __fsub_rn(qlo.y, hi.y)), 0.f);
-                            const float gz =
-                                D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, qhi.z), __fsub_rn(qlo.z, hi.z)), 0.f) : 0.f;
-                            lb = d2_of<D>(gx, gy, gz);
-                        }
+                        const uint32_t nlb = __ldg(&nlab[node]);
+                        const float4 lo = __ldg(&nlo[node]), hi = __ldg(&nhi[node]);
+                        const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, qhi.x), __fsub_rn(qlo.x, hi.x)), 0.f);
+                        const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, qhi.y), __fsub_rn(qlo.y, hi.y)), 0.f);
+                        const float gz =
+                            D == 3 ? fmaxf(fmaxf(__fsub_rn(lo.z, qhi.z), __fsub_rn(qlo.z, hi.z)), 0.f) : 0.f;
+                        lb = nlb != lab0 ? d2_of<D>(gx, gy, gz) : INFINITY;
                     }
                     const bool want = lb <= B, is_leaf = node >= L;
                     if (!want) dropped = fminf(dropped, lb);  // +inf: empty or the component's own
@@ -1428,7 +1438,6 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
         }
         // round-1 result: entry 0 (exact: every node within the K-th
         // distance was searched)
-        bool record = false;
         if (listed) {
             const int op = __float_as_int(P.w);
             if (kk[0] != kNoKey) {
@@ -1438,16 +1447,16 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 a.lbp[me] = d0;
                 a.selq[me] = p0;
                 a.selkey[me] = key;
-                // round 1: every point is its own component, the only writer of its key
+                // round 1: every point is its own component, the only writer
+                // of its key, and its own winner: the slot k_resolve would
+                // fill, (larger input id of the edge << 32 | position)
                 a.ckey[me] = key;
-                record = true;
+                a.cmax[me] = ((uint64_t)max((uint32_t)op, (uint32_t)kk[0]) << 32) | me;
             } else {
                 a.lbp[me] = INFINITY;  // alone in its cloud
                 a.selq[me] = kNone;
             }
         }
-        __syncwarp();
-        warp_append(record, me, a.prov, a.n_prov);
         if (a.stats) {
             // leaves, nodes and insert steps are per warp; candidates per listed lane
             unsigned long long q = __popc(__ballot_sync(kFull, listed));

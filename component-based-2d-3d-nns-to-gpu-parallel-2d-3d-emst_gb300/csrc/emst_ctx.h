@@ -316,6 +316,9 @@ struct CnnsArgs {
     uint32_t* trace_ctl;
     uint64_t trace_cap;
     uint32_t trace_mask;
+    // round-1 list build: per point the winner slot k_resolve would fill (the
+    // component is the point alone, so its own result is the winner)
+    uint64_t* cmax;
 };
 
 // Search counters of profile contexts (emst_profile): 0 leaves, 1 node tests,
