@@ -118,17 +118,37 @@ read once."""
 PHASES = ["ms_grid", "ms_octants", "ms_select", "ms_resolve", "ms_hook", "ms_flatten"]
 
 
-def traffic_from_profile(name):
-    """Mean DRAM bytes (read + write) per launch of the dominant kernel, from the
-    committed ncu summary profiles/<kernel>_<workload>.md (null if absent)."""
+def profile_value(name, key):
+    """A figure from a committed ncu summary profiles/<name>.md: the line
+    '<key>: <value>' (null if absent)."""
     path = os.path.join(ROOT, "profiles", "%s.md" % name)
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def traffic_from_profile(name):
+    """Mean DRAM bytes (read + write) per launch of the dominant kernel, from the
+    committed ncu summary profiles/<kernel>_<workload>.md (null if absent)."""
+    return profile_value(name, "traffic_bytes_per_launch")
+
+
+def issue_from_profile(kernel):
+    """What bounds an instruction-bound search kernel, from its committed full
+    ncu section set (profiles/<kernel>_gauss3d_4e6.md): issue-slot use, warp
+    instructions per 32 queries and active lanes per instruction."""
+    name = "%s_gauss3d_4e6" % kernel
+    busy = profile_value(name, "issue_slots_busy")
+    if busy is None:
+        return None
+    return {"bound": "instruction issue", "issue_slots_busy": busy,
+            "warp_instructions_per_32_queries": profile_value(name, "warp_instructions_per_32_queries"),
+            "active_lanes_per_instruction": profile_value(name, "active_lanes_per_instruction"),
+            "source": "ncu --set full of the same kernel on 4e6 points of the same generator (profiles/%s.md)" % name}
 
 
 def cpu_baseline(pts, threads, sample_n, seed=0, with_edges=False):
@@ -509,6 +529,7 @@ def main():
         alg = nns_bytes(n, dim) * K / n_launch
     achieved = alg / (per_launch_ms / 1e3) / 1e9
     traffic = traffic_from_profile("%s_%s" % (kernel, args.workload)) if args.n is None else None
+    issue = issue_from_profile(kernel) if args.workload.startswith("gauss3d") else None
     search = {"leaf_visits_per_warp": stat["leaf_visits"] / max(stat["search_warps"], 1),
               "node_tests_per_warp": stat["node_tests"] / max(stat["search_warps"], 1),
               "candidates_per_point": stat["candidates"] / (n * K),
@@ -559,7 +580,7 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
                              "alg_bytes_per_launch": alg, "ms_per_launch": per_launch_ms,
-                             "peak_kind": peak_kind},
+                             "peak_kind": peak_kind, "issue": issue},
                 "phase_ms": phase_ms, "learned": learned, "static_table_mode": static, "batch512": batch,
                 "cpu_baseline": cpu,
                 "e2e": {"value": e2e, "unit": "Mpoints/s", "h2d_bytes_per_step": int(pts.nbytes),
