@@ -41,6 +41,9 @@ struct emst_ctx {
     std::vector<const void*> gkey;
     int64_t body_launches = 0;
     emst_tuning tuning = {};  // the last emst_autotune's stages
+    // emst_solve: the edge list's copy to the host runs here beside the length kernel
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_ev = nullptr;
 };
 
 namespace {
@@ -586,6 +589,8 @@ emst_status emst_destroy(emst_ctx* x)
     if (c.hctr) cudaFreeHost(c.hctr);
     if (c.hlen) cudaFreeHost(c.hlen);
     drop_graph(x);
+    if (x->side) cudaStreamDestroy(x->side);
+    if (x->side_ev) cudaEventDestroy(x->side_ev);
     if (c.own_stream) cudaStreamDestroy(c.own_stream);
     delete x;
     return EMST_OK;
@@ -872,10 +877,30 @@ emst_status emst_solve(emst_ctx* x, const float* points, int64_t n, int dim, int
     emst_status st = do_initialize(x, points, n, dim, 0);
     if (st != EMST_OK) return st;
     if ((st = do_run(x)) != EMST_OK) return st;
-    int64_t ne = 0;
-    if ((st = emst_evaluate(x, &ne, length)) != EMST_OK) return st;
+    if ((st = read_counters(x)) != EMST_OK) return st;
+    Ctx& c = x->c;
+    const int64_t ne = (int64_t)c.n_edges;
     if (n_edges) *n_edges = ne;
-    if (uv) return emst_get_edges(x, uv, nullptr, n > 1 ? n - 1 : 0, nullptr);
+    if (uv && ne > (n > 1 ? n - 1 : 0)) return set_err(x, EMST_EOVERFLOW, "edge buffer too small");
+    // The edge list goes to the host on a second stream while the length
+    // kernel runs on the context's stream (both only read the edges); one
+    // wait for both.
+    const bool copy = uv && ne > 0;
+    if (copy) {
+        if (!x->side) EMST_CUDA(x, cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking), "stream");
+        if (!x->side_ev) EMST_CUDA(x, cudaEventCreateWithFlags(&x->side_ev, cudaEventDisableTiming), "event");
+        EMST_CUDA(x, cudaEventRecord(x->side_ev, c.stream), "event");
+        EMST_CUDA(x, cudaStreamWaitEvent(x->side, x->side_ev, 0), "event");
+        EMST_CUDA(x, cudaMemcpyAsync(uv, c.edges.p, sizeof(int32_t) * 2 * ne, cudaMemcpyDeviceToHost, x->side),
+                  "get_edges");
+    }
+    if (length) {
+        EMST_CUDA(x, emst::evaluate_length(c, c.dlen.p), "evaluate");
+        EMST_CUDA(x, cudaMemcpyAsync(c.hlen, c.dlen.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream), "evaluate");
+    }
+    EMST_CUDA(x, cudaStreamSynchronize(c.stream), "sync");
+    if (copy) EMST_CUDA(x, cudaStreamSynchronize(x->side), "sync");
+    if (length) *length = *c.hlen;
     return EMST_OK;
 }
 
