@@ -1448,8 +1448,9 @@ __global__ void __launch_bounds__(kKnnWarps * 32, 4) k_knn_first(const CnnsArgs 
                 a.selq[me] = p0;
                 a.selkey[me] = key;
                 // round 1: every point is its own component, the only writer
-                // of its key, and its own winner: the slot k_resolve would
-                // fill, (larger input id of the edge << 32 | position)
+                // of its key, and its own winner; its winner slot holds what
+                // k_resolve would write: (larger input id of the edge) << 32
+                // | position
                 a.ckey[me] = key;
                 a.cmax[me] = ((uint64_t)max((uint32_t)op, (uint32_t)kk[0]) << 32) | me;
             } else {
