@@ -50,61 +50,69 @@ __device__ __forceinline__ uint32_t merge_label(uint32_t a, uint32_t b)
 // (the flatten step) every point's label is first replaced by its root's
 // root, lab[j] = par[lab[j]] (K_EMST_flatten_DST_1, EMSTOperators.h:412-433),
 // so the relabel and the next round's node labels take one pass over lab.
+// Warp w takes the block's leaves [32 w, 32 w + 32), lane i keeps leaf
+// 32 w + i's label, and the subtree is merged by warp shuffles: five levels in
+// every warp, then the levels above across the block's warps in warp 0 (one
+// barrier instead of two per level).
 __global__ void __launch_bounds__(1024)
     k_node_labels_sub(uint32_t* __restrict__ lab, const uint32_t* __restrict__ par, uint32_t n, uint32_t nchunk,
                       uint32_t L, uint32_t span, uint32_t* __restrict__ nlab)
 {
-    __shared__ uint32_t s[kLeavesPerBlock];
+    __shared__ uint32_t s_w[32];
     const uint32_t first = blockIdx.x * span;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t wl0 = 32u * (uint32_t)w;
     // four leaves per warp and step, their loads issued together (each leaf
     // is a chain of two dependent loads: the label, then its root)
     constexpr int kU = 4;
-    const uint32_t nw = blockDim.x >> 5;
-    for (uint32_t l0 = w; l0 < span; l0 += kU * nw) {
+    uint32_t v = kEmpty;  // lane i: the label of leaf wl0 + i
+    for (uint32_t s0 = 0; s0 < 32u && wl0 + s0 < span; s0 += kU) {
         uint32_t my[kU];
-        bool v[kU];
+        bool ok[kU];
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
-            const uint32_t l = l0 + (uint32_t)u * nw, c = first + l;
+            const uint32_t l = wl0 + s0 + (uint32_t)u, c = first + l;
             const uint32_t j = c * 32 + lane;
-            v[u] = l < span && c < nchunk && j < n;
-            my[u] = v[u] ? lab[j] : 0u;
+            ok[u] = l < span && c < nchunk && j < n;
+            my[u] = ok[u] ? lab[j] : 0u;
         }
         if (par) {
 #pragma unroll
             for (int u = 0; u < kU; ++u)
-                if (v[u]) my[u] = __ldcg(&par[my[u]]);
+                if (ok[u]) my[u] = __ldcg(&par[my[u]]);
         }
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
-            const uint32_t l = l0 + (uint32_t)u * nw, c = first + l;
+            const uint32_t l = wl0 + s0 + (uint32_t)u, c = first + l;
             if (l >= span) break;  // warp-uniform
-            if (par && v[u]) lab[c * 32 + lane] = my[u];
+            if (par && ok[u]) lab[c * 32 + lane] = my[u];
             uint32_t out = kEmpty;
             if (c < nchunk) {
                 const uint32_t f = __shfl_sync(kFull, my[u], 0);
-                out = __all_sync(kFull, !v[u] || my[u] == f) ? f : kMixed;
+                out = __all_sync(kFull, !ok[u] || my[u] == f) ? f : kMixed;
             }
-            if (lane == 0) {
-                s[l] = out;
-                nlab[L + c] = out;
-            }
+            if (lane == 0) nlab[L + c] = out;
+            if ((uint32_t)lane == s0 + (uint32_t)u) v = out;
         }
     }
+    // level k node of block leaf i: (L + first) / 2^k + i / 2^k (L + first is a
+    // multiple of span)
+    const uint32_t base = L + first;
+    for (int k = 1; k <= 5 && (1u << k) <= span; ++k) {
+        v = merge_label(v, __shfl_down_sync(kFull, v, 1u << (k - 1)));
+        const uint32_t i = wl0 + (uint32_t)lane;
+        if ((lane & ((1 << k) - 1)) == 0 && i < span) nlab[(base >> k) + (i >> k)] = v;
+    }
+    if (span <= 32u) return;  // block-uniform
+    if (lane == 0) s_w[w] = v;
     __syncthreads();
-    uint32_t base = (L + first);
-    for (uint32_t cnt = span >> 1; cnt >= 1; cnt >>= 1) {
-        base >>= 1;
-        uint32_t v = 0;
-        const bool act = threadIdx.x < cnt;
-        if (act) v = merge_label(s[2 * threadIdx.x], s[2 * threadIdx.x + 1]);
-        __syncthreads();
-        if (act) {
-            s[threadIdx.x] = v;
-            nlab[base + threadIdx.x] = v;
+    if (w == 0) {
+        const uint32_t nw = span >> 5;  // warps holding leaves
+        v = (uint32_t)lane < nw ? s_w[lane] : kEmpty;
+        for (int k = 6; (1u << k) <= span; ++k) {
+            v = merge_label(v, __shfl_down_sync(kFull, v, 1u << (k - 6)));
+            if ((lane & ((1 << (k - 5)) - 1)) == 0 && (uint32_t)lane < nw) nlab[(base >> k) + ((uint32_t)lane >> (k - 5))] = v;
         }
-        __syncthreads();
     }
 }
 
