@@ -7,10 +7,13 @@ restatement: the faithful ring search of the reference (emst_oracle.c) where
 it finishes in seconds, and the kd-tree Boruvka restatement (emst_kd_oracle.c,
 the same rounds, tie-break and union rule; pinned to the faithful one in
 tests/test_oracle_golden.py) at 10^6 and 10^7 points, where the faithful
-search's overfull cells take hours.  Bit-exact: the edges added in every
-round, the per-round edge counts and every point's final root; the tree
-length to 1e-9 relative (doubles summed in another order).
+search's overfull cells take up to an hour.  Bit-exact: the edges added in
+every round, the per-round edge counts and every point's final root; the tree
+length to 1e-9 relative (doubles summed in another order).  The faithful
+restatement's own full-size edge sets are pinned by their canonical hashes
+(tests/golden/full_size_edge_hashes.json).
 """
+import json
 import os
 
 import numpy as np
@@ -18,6 +21,9 @@ import pytest
 
 import emst_workloads as W
 import pyoracle as O
+from crosscheck_full import edge_hash
+
+GOLDEN_HASHES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_size_edge_hashes.json")
 
 pytestmark = pytest.mark.gpu
 
@@ -110,3 +116,17 @@ def test_full_size_neighbour_lists_vs_oracle(gpu_lib, workload):
     rid, rd2 = O.knn(sp, ids.shape[1])
     bad = np.flatnonzero((ids.astype(np.int64) != rid).any(axis=1) | (d2 != rd2).any(axis=1))
     assert len(bad) == 0, (len(bad), bad[:5])
+
+
+@pytest.mark.parametrize("name", sorted(json.load(open(GOLDEN_HASHES))["hashes"]))
+def test_full_size_edge_set_equals_the_faithful_restatement(gpu_lib, name):
+    """The faithful ring-search restatement needs 51 minutes for gauss3d_1e7
+    on 8 host threads, so its full-size edge sets are kept as canonical hashes
+    (tests/golden/full_size_edge_hashes.json, made by oracle/crosscheck_full.py);
+    the GPU's edge set of the same seeded points must hash the same."""
+    golden = json.load(open(GOLDEN_HASHES))["hashes"][name]
+    pts = W.make(name)
+    with gpu_lib.Emst() as e:
+        uv, _ = e.solve(pts)
+    assert len(uv) == len(pts) - 1
+    assert edge_hash(uv) == golden["edge_hash"]
