@@ -127,3 +127,23 @@ def test_kd_oracle_equals_faithful(kind, dim, n):
     assert np.array_equal(a.edge_round, b.edge_round)
     assert list(a.round_edges) == list(b.round_edges)
     assert np.array_equal(a.labels, b.labels)
+
+
+def test_full_size_golden_hash_is_the_faithful_oracles():
+    """The full-size golden hashes (tests/golden/full_size_edge_hashes.json)
+    hold while the seeded generator and the faithful restatement stay as they
+    were: bezier2d_1e7, the one the oracle solves in well under a minute on the
+    host cores, is solved again here and must hash the same."""
+    import json
+    import os
+
+    import emst_workloads as W
+    from crosscheck_full import edge_hash
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full_size_edge_hashes.json")
+    golden = json.load(open(path))["hashes"]["bezier2d_1e7"]["edge_hash"]
+    O.set_threads(os.cpu_count() or 1)
+    pts = W.make("bezier2d_1e7")
+    sp, _, _, _ = O.rescale(pts)
+    ref = O.emst(sp, "faithful")
+    assert edge_hash(ref.edges) == golden
